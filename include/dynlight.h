@@ -1,0 +1,293 @@
+/*
+ * dynlight GB300 baker: the C ABI.
+ *
+ * One blocking call bakes a scene on one GPU and returns what the reference's
+ *
+ *     pub fn bake(input: &BakeInput, options: &BakeOptions, progress: &BakeProgress)
+ *         -> Result<BakedScene, BakeError>                      (src/bake/baker.rs:27-31)
+ *
+ * returns: per mesh the `dynamic_triangles` words (src/bake/triangle_words.rs:1-13), the lights
+ * in light-BVH slot order (src/bake/baker.rs:41-50), the light BVH nodes
+ * (src/bake/light_bvh.rs:16-22) and the bake statistics (src/bake/format/types.rs:205-222).
+ * Every struct is plain data with explicit sizes so a Rust `#[repr(C)]` mirror binds it
+ * directly; no C++ or CUDA type crosses the boundary, and no exception leaves it.
+ *
+ * Ownership: the caller owns every input array, which is read during the call only. Results
+ * live in a library allocation freed with dl_baked_scene_free(). Device memory is owned by the
+ * library. One bake runs at a time per process; a second concurrent call returns DL_BUSY.
+ */
+#ifndef DYNLIGHT_GB300_H
+#define DYNLIGHT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DL_ABI_VERSION 1u
+
+/* Status codes. The first five mirror BakeError (src/bake/input.rs:198-209). */
+typedef enum dl_status {
+    DL_OK = 0,
+    DL_CANCELLED = 1,       /* BakeError::Cancelled, through dl_progress.cancel */
+    DL_DUPLICATE_ID = 2,    /* BakeError::DuplicateId (src/bake/baker.rs:205-233) */
+    DL_INVALID_MESH = 3,    /* BakeError::InvalidMesh (src/bake/input.rs:233-287) */
+    DL_INVALID_LIGHT = 4,   /* BakeError::InvalidLight (src/bake/input.rs:290-323) */
+    DL_INVALID_OPTIONS = 5, /* BakeError::InvalidOptions (src/bake/input.rs:336-373) */
+    DL_CUDA_ERROR = 16,     /* a CUDA call failed; dl_last_error() names it */
+    DL_OUT_OF_MEMORY = 17,  /* device or host allocation failed */
+    DL_QUEUE_TIMEOUT = 18,  /* a bounded device wait gave up */
+    DL_BUSY = 19,           /* another bake is running in this process */
+    DL_UNSUPPORTED = 20,    /* a requested feature this library does not bake */
+    DL_INVALID_ARGUMENT = 21
+} dl_status;
+
+/* Light shape codes, as the .dynlight lights section stores them (src/bake/format/lights.rs:27-54). */
+typedef enum dl_light_shape {
+    DL_SHAPE_POINT = 0,
+    DL_SHAPE_RECTANGLE = 1,
+    DL_SHAPE_TUBE = 2,
+    DL_SHAPE_SUN = 3,
+    DL_SHAPE_SKY = 4
+} dl_light_shape;
+
+/* Illumination (src/light/kinds.rs:97-103). */
+enum { DL_ILLUMINATION_DIRECT = 0, DL_ILLUMINATION_SINGLE_BOUNCE = 1 };
+/* Transparency (src/light/kinds.rs:108-118): anything but Disabled alpha-tests shadow rays. */
+enum { DL_TRANSPARENCY_DISABLED = 0, DL_TRANSPARENCY_ENABLED = 1, DL_TRANSPARENCY_ENABLED_MAX = 2 };
+/* DynamicGeometryMode (src/shared/settings.rs:229-237). */
+enum { DL_GEOMETRY_LIGHTING_ONLY = 0, DL_GEOMETRY_DISTANCE_CUBES = 1, DL_GEOMETRY_ANGULAR = 2 };
+
+/* AlphaTexture (src/bake/input.rs:62-97): RGBA8 rows top to bottom. */
+typedef struct dl_alpha_texture {
+    uint32_t width;
+    uint32_t height;
+    const uint8_t *rgba8; /* width * height * 4 bytes */
+    float cutoff;
+    uint32_t reserved;
+} dl_alpha_texture;
+
+/* BakeMesh (src/bake/input.rs:24-45), world space. */
+typedef struct dl_mesh {
+    uint64_t id;               /* BakeId */
+    uint64_t content_hash;
+    uint32_t vertex_count;
+    uint32_t occludes;         /* 0 or 1 */
+    uint64_t index_count;      /* multiple of 3 */
+    const float *positions;    /* vertex_count * 3 */
+    const float *normals;      /* vertex_count * 3, or NULL for flat (face) normals */
+    const uint32_t *indices;   /* index_count */
+    const float *uv1;          /* vertex_count * 2: shadow map coordinates */
+    const float *uv0;          /* vertex_count * 2, or NULL */
+    const dl_alpha_texture *alpha; /* NULL: opaque; needs uv0 */
+    float albedo[3];           /* mean linear reflected color; colored bounce reads it */
+    uint32_t reserved;
+} dl_mesh;
+
+/* BakeLight (src/bake/input.rs:101-122) with its LightShape (src/light/shape.rs:19-30). */
+typedef struct dl_light {
+    uint64_t id;
+    float position[3];
+    float radius;
+    uint32_t illumination;       /* DL_ILLUMINATION_* */
+    uint32_t transparency;       /* DL_TRANSPARENCY_* */
+    uint32_t bounce_samples;     /* BakeBounce.samples (at least 2 are taken) */
+    float bounce_intensity;      /* BakeBounce.intensity */
+    int32_t bounce_compression;  /* bits per bounce pixel 8/6/5/4, or -1 for the options' */
+    uint32_t shape;              /* dl_light_shape */
+    float rotation[4];           /* quaternion x, y, z, w (rectangle, tube, sun) */
+    float size[2];               /* rectangle: width, height; tube: length, 0;
+                                    sun: angular diameter in degrees, 0 */
+} dl_light;
+
+typedef struct dl_bake_input {
+    const dl_mesh *meshes;
+    uint64_t mesh_count;
+    const dl_light *lights;
+    uint64_t light_count;
+} dl_bake_input;
+
+/* BakeOptions (src/bake/input.rs:136-164). */
+typedef struct dl_bake_options {
+    float pixel_density;
+    uint32_t max_lightmap_size;
+    uint32_t bounce_compression;     /* bits per pixel: 8, 6, 5 or 4 */
+    uint32_t dynamic_geometry;       /* DL_GEOMETRY_* */
+    uint32_t skip_bounce;
+    uint32_t photon_cube_resolution;
+    uint32_t area_light_samples;
+    uint32_t area_light_min_samples;
+    uint32_t sun_map_resolution;
+    uint32_t sky_samples;
+    float sky_probe_spacing;
+    uint32_t colored_bounce;
+    uint64_t seed;
+} dl_bake_options;
+
+/* BakeProgress (src/bake/progress.rs:41-110). The caller may set `cancel` from any thread;
+ * the library polls it between stages and the device work queue stops at its next item. */
+typedef struct dl_progress {
+    volatile uint32_t cancel;
+    volatile uint32_t stage; /* BakeStage order (src/bake/progress.rs:8-16) */
+    volatile uint64_t done;
+    volatile uint64_t total;
+} dl_progress;
+
+/* How the visibility stage runs. Both forms give identical bytes. */
+enum {
+    DL_FORM_BATCHED = 0, /* every (triangle, light) pair through one persistent kernel fed by a
+                            device work queue, launched from a CUDA graph */
+    DL_FORM_PLAIN = 1    /* one launch per (mesh, light): the reference's loop order on the GPU */
+};
+
+/* Launch configuration of one bake; zero-initialise for the defaults. */
+typedef struct dl_bake_config {
+    uint32_t form;             /* DL_FORM_* */
+    uint32_t device;           /* CUDA device ordinal */
+    uint32_t block_threads;    /* 0: tuned default */
+    uint32_t chunk_texels;     /* texels per work item of the batched queue, 0: default */
+    uint32_t sample_lanes;     /* lanes sharing one texel's soft/sky samples, 0: default */
+    uint32_t blocks_per_sm;    /* persistent blocks per SM, 0: default */
+    uint32_t reserved[8];
+} dl_bake_config;
+
+/* Timings (device events, milliseconds) and counters of the last bake. */
+typedef struct dl_bake_report {
+    double ms_total;          /* host wall clock of the whole call */
+    double ms_upload;         /* host -> device copies and BVH build */
+    double ms_device;         /* device time of the bake pipeline, events on its stream */
+    double ms_visibility;     /* device time of the visibility stage alone */
+    double ms_download;       /* device -> host copies and serialization */
+    uint64_t shadow_rays;     /* BakeStats.rays */
+    uint64_t bounce_rays;     /* BakeStats.bounce_rays */
+    uint64_t burial_rays;     /* closest-hit rays of the burial test */
+    uint64_t photon_rays;     /* closest-hit rays of the photon cubes */
+    uint64_t pairs;           /* (triangle, light) pairs traced */
+    uint64_t work_items;      /* items of the device work queue */
+    uint64_t kernel_launches; /* kernels this library launched for the bake */
+    uint64_t bvh_nodes;
+    uint64_t occluders;
+    uint64_t h2d_bytes;
+    uint64_t d2h_bytes;
+    uint64_t device_bytes;    /* peak device memory held by the bake */
+} dl_bake_report;
+
+/* LightBvhNode (src/bake/light_bvh.rs:16-22), 32 bytes. */
+typedef struct dl_light_bvh_node {
+    float aabb_min[3];
+    uint32_t left_first;
+    float aabb_max[3];
+    uint32_t count;
+} dl_light_bvh_node;
+
+/* BakedLight (src/bake/format/types.rs:161-175). */
+typedef struct dl_baked_light {
+    uint64_t id;
+    float origin[3];
+    float radius;
+    uint32_t shape;                 /* dl_light_shape */
+    float rotation[4];
+    float size[2];
+    uint32_t bounce_bits;           /* 0: no baked bounce */
+    uint32_t shadow_bits_per_texel; /* 1, 4 or 8 */
+} dl_baked_light;
+
+/* BakedMesh (src/bake/format/types.rs:178-190). */
+typedef struct dl_baked_mesh {
+    uint64_t id;
+    uint64_t content_hash;
+    uint32_t resolution;
+    uint32_t occludes;
+    const uint32_t *triangles; /* the mesh's dynamic_triangles words */
+    uint64_t word_count;
+} dl_baked_mesh;
+
+/* BakeStats (src/bake/format/types.rs:205-222). */
+typedef struct dl_bake_stats {
+    uint32_t meshes;
+    uint32_t reserved;
+    uint64_t triangles;
+    uint64_t texels;
+    uint64_t rays;
+    uint64_t lights_removed;
+    uint64_t bounce_rays;
+    uint64_t triangle_words;
+} dl_bake_stats;
+
+/* BakedSettings (src/bake/format/types.rs:128-145). */
+typedef struct dl_baked_settings {
+    uint32_t bounce;
+    uint32_t colored_bounce;
+    uint32_t dynamic_geometry;
+    float pixel_density;
+    uint32_t max_lightmap_size;
+    uint32_t distance_cube_resolution;
+} dl_baked_settings;
+
+/* BakedScene (src/bake/format/types.rs:13-37). Sun maps and sky probes are not baked here:
+ * with DL_GEOMETRY_LIGHTING_ONLY the reference leaves them empty too (src/bake/baker.rs:114-152). */
+typedef struct dl_baked_scene {
+    dl_baked_settings settings;
+    uint64_t light_count;
+    const dl_baked_light *lights;
+    uint64_t light_bvh_count;
+    const dl_light_bvh_node *light_bvh;
+    uint64_t mesh_count;
+    const dl_baked_mesh *meshes;
+    uint64_t distance_cube_words;
+    const uint32_t *distance_cubes;
+    dl_bake_stats stats;
+} dl_baked_scene;
+
+/* Library version, DL_ABI_VERSION. */
+uint32_t dl_abi_version(void);
+
+/* Human-readable name of a status. */
+const char *dl_status_string(dl_status status);
+
+/* Detail of the last failure on the calling thread (validation reason, CUDA error). */
+const char *dl_last_error(void);
+
+/* Replaces bake() (src/bake/baker.rs:27-203) with the batched form and default tuning.
+ * `progress` may be NULL. On DL_OK `*out` holds the result. */
+dl_status dl_bake(const dl_bake_input *input, const dl_bake_options *options,
+                  dl_progress *progress, dl_baked_scene **out);
+
+/* dl_bake with an explicit form and tuning; `report` (may be NULL) receives timings. */
+dl_status dl_bake_ex(const dl_bake_input *input, const dl_bake_options *options,
+                     const dl_bake_config *config, dl_progress *progress,
+                     dl_baked_scene **out, dl_bake_report *report);
+
+void dl_baked_scene_free(dl_baked_scene *scene);
+
+/* The reference's option defaults (BakeOptions::default, src/bake/input.rs:166-194 with
+ * BakeSettings::default, src/bake/settings.rs:67-81). */
+void dl_default_options(dl_bake_options *options);
+
+/* ---- Device-resident sessions: the same bake split at its host<->device boundaries, so a
+ * caller can repeat the device part on resident inputs (the benchmark's kernel-only number). */
+typedef struct dl_session dl_session;
+
+/* Validates and sorts the input, builds the light and occluder BVHs and uploads the scene. */
+dl_status dl_session_create(const dl_bake_input *input, const dl_bake_options *options,
+                            const dl_bake_config *config, dl_session **out);
+/* Runs every device stage of the bake on the resident scene; results stay on the device. */
+dl_status dl_session_run(dl_session *session, dl_progress *progress);
+/* Downloads the last run's results and serializes them. */
+dl_status dl_session_result(dl_session *session, dl_baked_scene **out);
+dl_status dl_session_report(const dl_session *session, dl_bake_report *report);
+void dl_session_destroy(dl_session *session);
+
+/* ---- .dynlight payload (src/bake/format/mod.rs:101-213): the uncompressed payload bytes and
+ * its CRC-32 (IEEE). The file's gzip layer is left to the caller's deflate library. */
+dl_status dl_encode_payload(const dl_baked_scene *scene, uint8_t **bytes, uint64_t *length,
+                            uint32_t *crc32);
+void dl_free(void *pointer);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DYNLIGHT_GB300_H */
