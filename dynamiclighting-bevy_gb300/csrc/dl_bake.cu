@@ -1,0 +1,1459 @@
+// The bake pipeline on one GPU and the C ABI (include/dynlight.h).
+//
+// Stages, all on one stream, each a kernel over the whole scene (every mesh at once):
+//   setup      per triangle: face normal, crop rect, light association (mesh_bake.rs:141-173)
+//   regions    per (mesh, light): union of crop rects -> one shadow grid (mesh_bake.rs:175-192)
+//   texels     per triangle: owned grid, centered + touched texels (texels.rs, mesh_texels.rs)
+//   burial     per texel: <= 8 closest-hit rays (mesh_texels.rs:57-88,111-135)
+//   visibility per (pair, texel): point/area/sun/sky shadow rays (mesh_bake.rs:203-267)
+//              batched: one persistent kernel over a device work queue, from a CUDA graph;
+//              plain: one launch per mesh, a warp per triangle, lanes over texels
+//   optimize   per triangle: drop lights with no lit texel nearby (shadows.rs:54-73)
+//   seams      per region: pad unvisited texels (seams.rs:15-39)
+//   serialize  per triangle/entry: header words, light data, cropped and dilated shadow words
+//              (shadows.rs:87-159, seams.rs:43-71, triangle_words.rs:47-89)
+// Sizes that decide later allocations are read back between stages (a handful of 8-byte copies).
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "dl_kernels.cuh"
+
+namespace dl {
+
+constexpr int kBlock = 128;
+constexpr uint32_t kNoRect = 0xFFFFFFFFu;
+constexpr uint64_t kBurialStream = 0x627572696564ull;  // mesh_texels.rs:26
+
+struct Counters {
+    unsigned long long rays, burial_rays, lights_removed, bounce_rays, photon_rays, cancelled;
+};
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// ================================ setup and association ==================================
+
+__global__ void k_setup(DevScene sc, float4 *tri_face, uint4 *tri_crop, uint32_t *tri_count) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= sc.triangles) return;
+    TriData d;
+    load_tri(sc, t, d);
+    f3 face = normalize_or_zero(cross(sub(d.v[1], d.v[0]), sub(d.v[2], d.v[0])));
+    uint32_t count = 0;
+    associate(sc, d, face, [&](uint32_t) { ++count; });
+    Rect c = crop_rect(d.uv, d.res);
+    tri_face[t] = make_float4(face.x, face.y, face.z, is_zero(face) ? 0.0f : 1.0f);
+    tri_crop[t] = make_uint4(c.min_x, c.min_y, c.max_x, c.max_y);
+    tri_count[t] = count;
+}
+
+__global__ void k_assoc_fill(DevScene sc, const float4 *tri_face, const uint4 *tri_crop, const uint32_t *tri_off,
+                             uint32_t *pair_light, uint32_t *pair_tri, uint32_t *region_rect) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= sc.triangles) return;
+    TriData d;
+    load_tri(sc, t, d);
+    float4 f = tri_face[t];
+    uint4 c = tri_crop[t];
+    uint32_t p = tri_off[t];
+    associate(sc, d, f3{f.x, f.y, f.z}, [&](uint32_t s) {
+        pair_light[p] = s;
+        pair_tri[p] = t;
+        ++p;
+        uint32_t *r = region_rect + ((size_t)d.mesh * sc.light_count + s) * 4;
+        atomicMin(r, c.x);
+        atomicMin(r + 1, c.y);
+        atomicMax(r + 2, c.z);
+        atomicMax(r + 3, c.w);
+    });
+}
+
+__global__ void k_fill_u32(uint32_t *p, size_t n, uint32_t a, uint32_t b) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = (i & 2) ? b : a;  // 4-word records (a, a, b, b)
+}
+
+// Words of each (mesh, light) region grid: bits for 1-bit lights, one byte per texel else.
+__global__ void k_region_words(const uint32_t *region_rect, const DevLight *lights, uint32_t entries, uint32_t L,
+                               uint32_t *words) {
+    uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e > entries) return;
+    if (e == entries) {
+        words[e] = 0;
+        return;
+    }
+    const uint32_t *r = region_rect + (size_t)e * 4;
+    if (r[0] == kNoRect) {
+        words[e] = 0;
+        return;
+    }
+    uint64_t n = (uint64_t)(r[2] - r[0] + 1) * (r[3] - r[1] + 1);
+    words[e] = lights[e % L].shadow_bits == 1 ? (uint32_t)((n + 31) / 32) : (uint32_t)((n + 3) / 4);
+}
+
+// ================================ texels ===============================================
+
+// MODE 0: count centered texels and set the owned grid; MODE 1: count touched texels;
+// MODE 2: write centered then touched texels at tex_off[t]. One warp per triangle.
+template <int MODE>
+__global__ void k_texels(DevScene sc, const float4 *tri_face, uint32_t *owned, const uint64_t *grid_off,
+                         uint32_t *count, const uint32_t *tex_off, uint32_t *tex_xy, float4 *tex_pos, float4 *tex_nrm,
+                         uint32_t *tex_tri) {
+    uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    unsigned lane = lane_id();
+    if (t >= sc.triangles) return;
+    float4 f = tri_face[t];
+    if (f.w == 0.0f) {
+        if (MODE != 2 && lane == 0) count[t] = 0;
+        return;
+    }
+    f3 face{f.x, f.y, f.z};
+    TriData d;
+    load_tri(sc, t, d);
+    uint32_t res = d.res;
+    uint32_t *own = owned + grid_off[d.mesh];
+    uint32_t written = 0;
+    uint32_t out = MODE == 2 ? tex_off[t] : 0;
+    if (MODE == 0 || MODE == 2) {
+        Rect r = center_rect(d.uv, res, 0.0f);
+        uint32_t w = r.max_x - r.min_x + 1;
+        uint64_t n = (uint64_t)w * (r.max_y - r.min_y + 1);
+        for (uint64_t base = 0; base < n; base += 32) {
+            uint64_t i = base + lane;
+            bool inside = false;
+            uint32_t x = 0, y = 0;
+            f3 wts;
+            if (i < n) {
+                x = r.min_x + (uint32_t)(i % w);
+                y = r.min_y + (uint32_t)(i / w);
+                inside = uv_barycentrics(d.uv, texel_center(x, y, res), wts);
+            }
+            unsigned ballot = __ballot_sync(0xFFFFFFFFu, inside);
+            if (inside) {
+                if (MODE == 0) {
+                    uint64_t bit = (uint64_t)x + (uint64_t)y * res;
+                    atomicOr(own + bit / 32, 1u << (bit % 32));
+                } else {
+                    uint32_t o = out + written + __popc(ballot & ((1u << lane) - 1u));
+                    f3 pos, nrm;
+                    surface_at(d, face, wts, pos, nrm);
+                    tex_xy[o] = x | (y << 16);
+                    tex_pos[o] = make_float4(pos.x, pos.y, pos.z, 0.0f);
+                    tex_nrm[o] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+                    tex_tri[o] = t;
+                }
+            }
+            written += __popc(ballot);
+        }
+        if (MODE == 0) {
+            if (lane == 0) count[t] = written;
+            return;
+        }
+    }
+    // touched texels (texels.rs:78-121)
+    float s = (float)res;
+    f2 mn, mx;
+    uv_bounds(d.uv, mn, mx);
+    uint32_t x0 = f2u(fmaxf(floorf(mn.x * s), 0.0f)), y0 = f2u(fmaxf(floorf(mn.y * s), 0.0f));
+    uint32_t x1 = f2u(fminf(floorf(mx.x * s), s - 1.0f)), y1 = f2u(fminf(floorf(mx.y * s), s - 1.0f));
+    float half = 0.5f / s;
+    uint32_t touched = 0;
+    if (x1 >= x0 && y1 >= y0) {
+        uint32_t w = x1 - x0 + 1;
+        uint64_t n = (uint64_t)w * (y1 - y0 + 1);
+        for (uint64_t base = 0; base < n; base += 32) {
+            uint64_t i = base + lane;
+            bool take = false;
+            uint32_t x = 0, y = 0;
+            f3 wts;
+            if (i < n) {
+                x = x0 + (uint32_t)(i % w);
+                y = y0 + (uint32_t)(i / w);
+                uint64_t bit = (uint64_t)x + (uint64_t)y * res;
+                bool is_owned = (own[bit / 32] >> (bit % 32)) & 1u;
+                if (!is_owned) {
+                    f2 center = texel_center(x, y, res);
+                    if (nearest_weights(d.uv, center, wts)) {
+                        float nx = d.uv[0].x * wts.x + d.uv[1].x * wts.y + d.uv[2].x * wts.z;
+                        float ny = d.uv[0].y * wts.x + d.uv[1].y * wts.y + d.uv[2].y * wts.z;
+                        take = fmaxf(fabsf(nx - center.x), fabsf(ny - center.y)) <= half;
+                    }
+                }
+            }
+            unsigned ballot = __ballot_sync(0xFFFFFFFFu, take);
+            if (MODE == 2 && take) {
+                uint32_t o = out + written + touched + __popc(ballot & ((1u << lane) - 1u));
+                f3 pos, nrm;
+                surface_at(d, face, wts, pos, nrm);
+                tex_xy[o] = x | (y << 16);
+                tex_pos[o] = make_float4(pos.x, pos.y, pos.z, 0.0f);
+                tex_nrm[o] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+                tex_tri[o] = t;
+            }
+            touched += __popc(ballot);
+        }
+    }
+    if (MODE == 1 && lane == 0) count[t] = touched;
+}
+
+// Burial test per texel (mesh_texels.rs:57-88). Buried texels are dropped from tracing.
+__global__ void __launch_bounds__(kBlock) k_burial(DevScene sc, uint32_t texels, const uint32_t *tex_xy,
+                                                   const float4 *tex_pos, const uint32_t *tex_tri,
+                                                   const float4 *tri_face, uint8_t *buried, Counters *ctr) {
+    __shared__ int stack[kStack * kBlock];
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t rays = 0;
+    if (i < texels) {
+        uint32_t t = tex_tri[i];
+        uint32_t m = sc.tri_mesh[t];
+        float4 f = tri_face[t], p = tex_pos[i];
+        f3 normal{f.x, f.y, f.z};
+        uint32_t xy = tex_xy[i];
+        f3 origin = add(f3{p.x, p.y, p.z}, scale(normal, kRayOffset));
+        Pcg rng = stream6(sc.seed, sc.mesh_id[m], kBurialStream, t - sc.mesh_tri_base[m], xy & 0xFFFFu, xy >> 16);
+        float turn = rng.next_f32();
+        buried[i] = is_buried(sc, normal, origin, turn, stack + threadIdx.x, kBlock, rays) ? 1 : 0;
+    }
+    unsigned r = __reduce_add_sync(0xFFFFFFFFu, rays);
+    if (lane_id() == 0 && r) atomicAdd(&ctr->burial_rays, (unsigned long long)r);
+}
+
+__global__ void k_add_u32(const uint32_t *a, const uint32_t *b, uint32_t *c, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) c[i] = a[i] + b[i];
+    if (i == n) c[i] = 0;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+
+// Per triangle: how many of its texels are not buried (warp per triangle).
+template <bool WRITE>
+__global__ void k_unburied(uint32_t triangles, const uint32_t *tex_off, const uint8_t *buried, uint32_t *count,
+                           const uint32_t *ctex_off, const uint32_t *tex_xy, const float4 *tex_pos,
+                           const float4 *tex_nrm, uint32_t *c_xy, float4 *c_pos, float4 *c_nrm) {
+    uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    unsigned lane = lane_id();
+    if (t >= triangles) return;
+    uint32_t b = tex_off[t], e = tex_off[t + 1];
+    uint32_t kept = 0;
+    uint32_t out = WRITE ? ctex_off[t] : 0;
+    for (uint32_t base = b; base < e; base += 32) {
+        uint32_t i = base + lane;
+        bool keep = i < e && !buried[i];
+        unsigned ballot = __ballot_sync(0xFFFFFFFFu, keep);
+        if (WRITE && keep) {
+            uint32_t o = out + kept + __popc(ballot & ((1u << lane) - 1u));
+            c_xy[o] = tex_xy[i];
+            c_pos[o] = tex_pos[i];
+            c_nrm[o] = tex_nrm[i];
+        }
+        kept += __popc(ballot);
+    }
+    if (!WRITE && lane == 0) count[t] = kept;
+}
+
+// ================================ visibility ===========================================
+
+struct TraceArgs {
+    const uint32_t *pair_tri, *pair_light;
+    const uint32_t *ctex_off, *ctex_xy;
+    const float4 *ctex_pos, *ctex_nrm, *tri_face;
+    const uint64_t *grid_off;  // visited grid word offset per mesh
+    uint32_t *visited;
+    const uint32_t *region_rect, *region_off;
+    uint32_t *region_pool;
+    Counters *ctr;
+    // batched queue
+    const uint32_t *order, *item_off;
+    uint32_t pairs;
+    unsigned long long items;
+    unsigned long long *head;
+    const volatile uint32_t *cancel;
+    uint32_t grab;
+};
+
+// One (pair, texel) of the visibility loop (mesh_bake.rs:231-248); returns the rays traced.
+__device__ __forceinline__ uint32_t trace_texel(const DevScene &sc, const TraceArgs &a, uint32_t p, uint32_t k,
+                                                int *stack, int stride) {
+    uint32_t t = a.pair_tri[p], s = a.pair_light[p];
+    uint32_t m = sc.tri_mesh[t];
+    uint32_t ci = a.ctex_off[t] + k;
+    uint32_t xy = a.ctex_xy[ci];
+    uint32_t x = xy & 0xFFFFu, y = xy >> 16;
+    float4 pp = a.ctex_pos[ci], nn = a.ctex_nrm[ci], f = a.tri_face[t];
+    f3 pos{pp.x, pp.y, pp.z}, nrm{nn.x, nn.y, nn.z};
+    f3 origin = add(pos, scale(f3{f.x, f.y, f.z}, kRayOffset));
+    const DevLight &l = sc.lights[s];
+    Tracer tr{sc, origin, (l.flags & kLightAlpha) != 0, stack, stride};
+    Vis v = texel_shadow(sc, s, sc.mesh_id[m], x, y, pos, nrm, tr);
+    if (!v.some) return 0;
+    uint32_t res = sc.mesh_res[m];
+    uint64_t bit = (uint64_t)x + (uint64_t)y * res;
+    atomicOr(a.visited + a.grid_off[m] + bit / 32, 1u << (bit % 32));
+    size_t e = (size_t)m * sc.light_count + s;
+    const uint32_t *r = a.region_rect + e * 4;
+    uint32_t w = r[2] - r[0] + 1;
+    uint64_t idx = (uint64_t)(x - r[0]) + (uint64_t)(y - r[1]) * w;
+    uint32_t *g = a.region_pool + a.region_off[e];
+    if (l.shadow_bits == 1) {
+        if (v.level) atomicOr(g + idx / 32, 1u << (idx % 32));
+    } else if (v.level) {
+        uint32_t *word = g + idx / 4;
+        uint32_t shift = (uint32_t)(idx % 4) * 8;
+        uint32_t cur = *word;
+        for (;;) {
+            if (((cur >> shift) & 0xFFu) >= v.level) break;
+            uint32_t want = (cur & ~(0xFFu << shift)) | (v.level << shift);
+            uint32_t prev = atomicCAS(word, cur, want);
+            if (prev == cur) break;
+            cur = prev;
+        }
+    }
+    return v.rays;
+}
+
+// Batched form: persistent warps pull chunks of (pair, texel) items from one queue. Items are
+// ordered sky pairs first, then soft, then hard, so the longest work starts first.
+__global__ void __launch_bounds__(kBlock) k_trace_batched(DevScene sc, TraceArgs a) {
+    __shared__ int stack[kStack * kBlock];
+    int *my = stack + threadIdx.x;
+    unsigned lane = lane_id();
+    unsigned long long rays = 0;
+    uint32_t grabs = 0;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) {
+            base = atomicAdd(a.head, (unsigned long long)(32 * a.grab));
+            if ((++grabs & 15u) == 0 && *a.cancel) base = a.items;
+        }
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= a.items) break;
+        // the chunk's first pair: item_off[lo] <= base < item_off[lo + 1]
+        uint32_t lo = 0, hi = a.pairs;
+        while (hi - lo > 1) {
+            uint32_t mid = (lo + hi) >> 1;
+            if ((unsigned long long)a.item_off[mid] <= base) lo = mid;
+            else hi = mid;
+        }
+        uint32_t cur = lo;  // per lane, advances monotonically over the chunk
+        for (uint32_t g = 0; g < a.grab; ++g) {
+            unsigned long long item = base + (unsigned long long)g * 32 + lane;
+            if (item < a.items) {
+                while ((unsigned long long)a.item_off[cur + 1] <= item) ++cur;
+                rays += trace_texel(sc, a, a.order[cur], (uint32_t)(item - a.item_off[cur]), my, kBlock);
+            }
+        }
+    }
+    unsigned long long r = warp_sum(rays);
+    if (lane == 0 && r) atomicAdd(&a.ctr->rays, r);
+}
+
+// Plain form: one launch per mesh; a warp per triangle, its lights in order, lanes over texels.
+__global__ void __launch_bounds__(kBlock) k_trace_plain(DevScene sc, TraceArgs a, uint32_t first_tri,
+                                                         uint32_t tri_count, const uint32_t *tri_pair_off) {
+    __shared__ int stack[kStack * kBlock];
+    int *my = stack + threadIdx.x;
+    unsigned lane = lane_id();
+    unsigned long long rays = 0;
+    uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < tri_count; w += warps) {
+        uint32_t t = first_tri + w;
+        uint32_t n = a.ctex_off[t + 1] - a.ctex_off[t];
+        for (uint32_t p = tri_pair_off[t]; p < tri_pair_off[t + 1]; ++p)
+            for (uint32_t k = lane; k < n; k += 32) rays += trace_texel(sc, a, p, k, my, kBlock);
+    }
+    unsigned long long r = warp_sum(rays);
+    if (lane == 0 && r) atomicAdd(&a.ctr->rays, r);
+}
+
+// Queue construction: pairs in class order (sky, soft, hard) and their item prefix sums.
+__global__ void k_pair_class(DevScene sc, const uint32_t *pair_light, uint32_t pairs, uint32_t cls, uint32_t *flag) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p > pairs) return;
+    if (p == pairs) {
+        flag[p] = 0;
+        return;
+    }
+    const DevLight &l = sc.lights[pair_light[p]];
+    uint32_t c = l.shape == DL_SHAPE_SKY ? 0 : (l.shadow_bits > 1 ? 1 : 2);
+    flag[p] = c == cls;
+}
+__global__ void k_pair_scatter(const uint32_t *flag, const uint32_t *pos, uint32_t pairs, uint32_t base,
+                               uint32_t *order) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < pairs && flag[p]) order[base + pos[p]] = p;
+}
+__global__ void k_item_counts(const uint32_t *order, const uint32_t *pair_tri, const uint32_t *ctex_off,
+                              uint32_t pairs, uint32_t *cnt) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > pairs) return;
+    if (i == pairs) {
+        cnt[i] = 0;
+        return;
+    }
+    uint32_t t = pair_tri[order[i]];
+    cnt[i] = ctex_off[t + 1] - ctex_off[t];
+}
+
+// ================================ optimize, seams, serialize ===========================
+
+__device__ __forceinline__ uint32_t region_get(const uint32_t *pool, uint32_t off, const uint32_t *r, uint32_t bits,
+                                               int64_t x, int64_t y) {
+    if (x < (int64_t)r[0] || y < (int64_t)r[1] || x > (int64_t)r[2] || y > (int64_t)r[3]) return 0;
+    uint64_t w = r[2] - r[0] + 1;
+    uint64_t idx = (uint64_t)(x - r[0]) + (uint64_t)(y - r[1]) * w;
+    if (bits == 1) return (pool[off + idx / 32] >> (idx % 32)) & 1u;
+    return (pool[off + idx / 4] >> ((idx % 4) * 8)) & 0xFFu;
+}
+
+// LightEntries::optimize (shadows.rs:54-73) + any_light (:136-144); marks used regions.
+__global__ void k_optimize(DevScene sc, const uint32_t *tri_off, const uint32_t *pair_light,
+                           const uint32_t *region_rect, const uint32_t *region_off, const uint32_t *region_pool,
+                           const uint8_t *pair_bounce, uint8_t *keep, uint32_t *kept_count, uint8_t *used,
+                           Counters *ctr) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= sc.triangles) return;
+    TriData d;
+    load_tri(sc, t, d);
+    Rect o = center_rect(d.uv, d.res, 1.0f);
+    uint32_t kept = 0, removed = 0;
+    for (uint32_t p = tri_off[t]; p < tri_off[t + 1]; ++p) {
+        uint32_t s = pair_light[p];
+        size_t e = (size_t)d.mesh * sc.light_count + s;
+        bool k = pair_bounce && pair_bounce[p];
+        if (!k) {
+            const uint32_t *r = region_rect + e * 4;
+            uint32_t min_x = max(o.min_x, r[0]), max_x = min(o.max_x, r[2]);
+            uint32_t min_y = max(o.min_y, r[1]), max_y = min(o.max_y, r[3]);
+            uint32_t bits = sc.lights[s].shadow_bits;
+            for (uint32_t y = min_y; y <= max_y && !k && min_x <= max_x; ++y)
+                for (uint32_t x = min_x; x <= max_x && !k; ++x)
+                    k = region_get(region_pool, region_off[e], r, bits, x, y) != 0;
+        }
+        keep[p] = k;
+        if (k) {
+            ++kept;
+            used[e] = 1;
+        } else {
+            ++removed;
+        }
+    }
+    kept_count[t] = kept;
+    if (removed) atomicAdd(&ctr->lights_removed, (unsigned long long)removed);
+}
+
+// pad_seams (seams.rs:15-39) on every used region; a block per (mesh, light) entry.
+__global__ void k_pad_seams(DevScene sc, const uint8_t *used, const uint32_t *region_rect, const uint32_t *region_off,
+                            uint32_t *region_pool, const uint32_t *visited, const uint64_t *grid_off) {
+    size_t e = blockIdx.x;
+    if (!used[e]) return;
+    const uint32_t *r = region_rect + e * 4;
+    uint32_t m = (uint32_t)(e / sc.light_count), s = (uint32_t)(e % sc.light_count);
+    uint32_t res = sc.mesh_res[m];
+    const uint32_t *vis = visited + grid_off[m];
+    uint32_t bits = sc.lights[s].shadow_bits;
+    uint32_t off = region_off[e];
+    uint32_t w = r[2] - r[0] + 1, h = r[3] - r[1] + 1;
+    auto visited_at = [&](int64_t x, int64_t y) -> bool {
+        if (x < 0 || y < 0 || x >= (int64_t)res || y >= (int64_t)res) return false;
+        uint64_t bit = (uint64_t)x + (uint64_t)y * res;
+        return (vis[bit / 32] >> (bit % 32)) & 1u;
+    };
+    const int dxs[4] = {-1, 1, 0, 0}, dys[4] = {0, 0, -1, 1};
+    for (uint64_t i = threadIdx.x; i < (uint64_t)w * h; i += blockDim.x) {
+        int64_t x = r[0] + (int64_t)(i % w), y = r[1] + (int64_t)(i / w);
+        if (visited_at(x, y)) continue;
+        uint32_t level = 0;
+        for (int k = 0; k < 4; ++k) {
+            int64_t nx = x + dxs[k], ny = y + dys[k];
+            if (visited_at(nx, ny))
+                level = max(level, region_get(region_pool, off, r, bits, nx, ny));
+            else if (visited_at(x + 2 * dxs[k], y + 2 * dys[k]))
+                level = max(level, region_get(region_pool, off, r, bits, x + 2 * dxs[k], y + 2 * dys[k]));
+        }
+        if (!level) continue;  // unvisited texels hold 0 already
+        if (bits == 1)
+            atomicOr(region_pool + off + i / 32, 1u << (i % 32));
+        else
+            reinterpret_cast<uint8_t *>(region_pool + off)[i] = (uint8_t)level;
+    }
+}
+
+__device__ __forceinline__ uint64_t shadow_words(uint4 crop, uint32_t bits) {
+    uint64_t n = (uint64_t)(crop.z - crop.x + 5) * (crop.w - crop.y + 5);
+    uint32_t per = 32 / bits;
+    return (n + per - 1) / per;
+}
+
+// Words per triangle: light data (1 + stride per kept light) and payload.
+__global__ void k_tri_words(DevScene sc, const uint32_t *tri_off, const uint32_t *pair_light, const uint8_t *keep,
+                            const uint4 *tri_crop, uint32_t stride, unsigned long long *ld_words,
+                            unsigned long long *pl_words) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > sc.triangles) return;
+    if (t == sc.triangles) {
+        ld_words[t] = pl_words[t] = 0;
+        return;
+    }
+    uint4 c = tri_crop[t];
+    unsigned long long ld = 1, pl = 0;
+    for (uint32_t p = tri_off[t]; p < tri_off[t + 1]; ++p)
+        if (keep[p]) {
+            ld += stride;
+            pl += shadow_words(c, sc.lights[pair_light[p]].shadow_bits);
+        }
+    ld_words[t] = ld;
+    pl_words[t] = pl;
+}
+
+__global__ void k_mesh_words(DevScene sc, const unsigned long long *ld_scan, const unsigned long long *pl_scan,
+                             unsigned long long *mesh_words) {
+    uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m > sc.mesh_count) return;
+    if (m == sc.mesh_count) {
+        mesh_words[m] = 0;
+        return;
+    }
+    uint32_t a = sc.mesh_tri_base[m], b = sc.mesh_tri_base[m + 1];
+    mesh_words[m] = 4ull * (b - a) + (ld_scan[b] - ld_scan[a]) + (pl_scan[b] - pl_scan[a]);
+}
+
+// serialize_triangles (triangle_words.rs:47-89): headers, light data, and where each kept
+// entry's shadow words go.
+__global__ void k_serialize(DevScene sc, const uint32_t *tri_off, const uint32_t *pair_light, const uint8_t *keep,
+                            const uint4 *tri_crop, uint32_t stride, const unsigned long long *ld_scan,
+                            const unsigned long long *pl_scan, const unsigned long long *mesh_base,
+                            const uint32_t *entry_off, uint32_t *words, uint32_t *entry_pair,
+                            unsigned long long *entry_dst) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= sc.triangles) return;
+    uint32_t m = sc.tri_mesh[t];
+    uint32_t first = sc.mesh_tri_base[m], tris = sc.mesh_tri_base[m + 1] - first;
+    unsigned long long base = mesh_base[m];
+    uint32_t ld_total = (uint32_t)(ld_scan[first + tris] - ld_scan[first]);
+    uint32_t ld = 4 * tris + (uint32_t)(ld_scan[t] - ld_scan[first]);
+    uint32_t pl = 4 * tris + ld_total + (uint32_t)(pl_scan[t] - pl_scan[first]);
+    uint4 c = tri_crop[t];
+    uint32_t lt = t - first;
+    words[base + 4 * lt] = ld;
+    words[base + 4 * lt + 1] = c.x - 2u;
+    words[base + 4 * lt + 2] = c.y - 2u;
+    words[base + 4 * lt + 3] = c.z - c.x + 5;
+    uint32_t count = 0;
+    uint32_t e = entry_off[t];
+    for (uint32_t p = tri_off[t]; p < tri_off[t + 1]; ++p) {
+        if (!keep[p]) continue;
+        uint32_t s = pair_light[p];
+        uint32_t at = ld + 1 + count * stride;
+        words[base + at] = s;
+        words[base + at + 1] = pl;
+        if (stride == 3) words[base + at + 2] = 0;
+        entry_pair[e] = p;
+        entry_dst[e] = base + pl;
+        pl += (uint32_t)shadow_words(c, sc.lights[s].shadow_bits);
+        ++count;
+        ++e;
+    }
+    words[base + ld] = count;
+}
+
+// crop_shadows (shadows.rs:148-159) with dilate_shadows (seams.rs:43-71), packed as
+// ShadowGrid::into_words (shadow_grid.rs:91-106). A warp per kept entry, a lane per word; every
+// texel of the padded grid is computed from the region directly:
+//   interior: the region's level; inner ring: 3x3 max of the interior; outer ring: 3x3 max of
+//   interior and inner ring.
+__device__ __forceinline__ uint32_t crop_level(const uint32_t *pool, uint32_t off, const uint32_t *r, uint32_t bits,
+                                               uint4 c, int gw, int gh, int gx, int gy) {
+    auto interior = [&](int x, int y) -> uint32_t {
+        if (x < 2 || y < 2 || x >= gw - 2 || y >= gh - 2) return 0;
+        return region_get(pool, off, r, bits, (int64_t)c.x + x - 2, (int64_t)c.y + y - 2);
+    };
+    auto inner = [&](int x, int y) -> uint32_t {
+        uint32_t v = 0;
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) v = max(v, interior(x + dx, y + dy));
+        return v;
+    };
+    bool outer = gx == 0 || gy == 0 || gx == gw - 1 || gy == gh - 1;
+    if (outer) {
+        uint32_t v = 0;
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                int x = gx + dx, y = gy + dy;
+                if (x < 0 || y < 0 || x >= gw || y >= gh) continue;
+                bool ring = x == 0 || y == 0 || x == gw - 1 || y == gh - 1;
+                if (ring) continue;  // outer ring cells are 0 after the first pass
+                bool in_ring = x == 1 || y == 1 || x == gw - 2 || y == gh - 2;
+                v = max(v, in_ring ? inner(x, y) : interior(x, y));
+            }
+        return v;
+    }
+    bool in_ring = gx == 1 || gy == 1 || gx == gw - 2 || gy == gh - 2;
+    return in_ring ? inner(gx, gy) : interior(gx, gy);
+}
+
+__global__ void k_crop(DevScene sc, uint32_t entries, const uint32_t *entry_pair, const unsigned long long *entry_dst,
+                       const uint32_t *pair_tri, const uint32_t *pair_light, const uint4 *tri_crop,
+                       const uint32_t *region_rect, const uint32_t *region_off, const uint32_t *region_pool,
+                       uint32_t *words) {
+    uint32_t e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    unsigned lane = lane_id();
+    if (e >= entries) return;
+    uint32_t p = entry_pair[e];
+    uint32_t t = pair_tri[p], s = pair_light[p];
+    uint32_t m = sc.tri_mesh[t];
+    uint4 c = tri_crop[t];
+    size_t re = (size_t)m * sc.light_count + s;
+    const uint32_t *r = region_rect + re * 4;
+    uint32_t off = region_off[re];
+    uint32_t bits = sc.lights[s].shadow_bits;
+    int gw = (int)(c.z - c.x + 5), gh = (int)(c.w - c.y + 5);
+    uint64_t n = (uint64_t)gw * gh;
+    uint32_t per = 32 / bits;
+    uint64_t nw = (n + per - 1) / per;
+    unsigned long long dst = entry_dst[e];
+    for (uint64_t wi = lane; wi < nw; wi += 32) {
+        uint32_t word = 0;
+        for (uint32_t j = 0; j < per; ++j) {
+            uint64_t i = wi * per + j;
+            if (i >= n) break;
+            uint32_t v = crop_level(region_pool, off, r, bits, c, gw, gh, (int)(i % gw), (int)(i / gw));
+            word |= (bits == 1 ? (v != 0) : v) << (j * bits);
+        }
+        words[dst + wi] = word;
+    }
+}
+
+// ================================ host side =================================================
+
+namespace {
+
+thread_local std::string g_error;
+std::mutex g_busy;
+
+struct CudaError {
+    cudaError_t code;
+    const char *what;
+};
+
+#define CK(x)                                                      \
+    do {                                                           \
+        cudaError_t e__ = (x);                                     \
+        if (e__ != cudaSuccess) throw CudaError{e__, #x};          \
+    } while (0)
+
+template <class T>
+T *dev_alloc(std::vector<void *> &owned, size_t count, uint64_t &bytes) {
+    void *p = nullptr;
+    size_t b = std::max<size_t>(count * sizeof(T), 16);
+    CK(cudaMalloc(&p, b));
+    owned.push_back(p);
+    bytes += b;
+    return static_cast<T *>(p);
+}
+
+double ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+
+// A named pool of device buffers, grown on demand and reused across runs of one session.
+struct Pool {
+    std::map<std::string, std::pair<void *, size_t>> bufs;
+    uint64_t bytes = 0;
+    uint64_t generation = 0;  // bumped whenever a buffer moves
+    template <class T>
+    T *get(const std::string &name, size_t count) {
+        size_t b = std::max<size_t>(count * sizeof(T), 16);
+        auto it = bufs.find(name);
+        if (it != bufs.end() && it->second.second >= b) return static_cast<T *>(it->second.first);
+        if (it != bufs.end()) {
+            cudaFree(it->second.first);
+            bytes -= it->second.second;
+        }
+        void *p = nullptr;
+        CK(cudaMalloc(&p, b));
+        bufs[name] = {p, b};
+        bytes += b;
+        ++generation;
+        return static_cast<T *>(p);
+    }
+    ~Pool() {
+        for (auto &kv : bufs) cudaFree(kv.second.first);
+    }
+};
+
+}  // namespace dl
+
+using namespace dl;
+
+struct dl_session {
+    HostScene host;
+    dl_bake_options options{};
+    dl_bake_config config{};
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr, side = nullptr;
+    std::vector<void *> owned;
+    uint64_t scene_bytes = 0;
+    DevScene sc{};
+    std::vector<uint64_t> grid_off;  // visited/owned word offset per mesh
+    uint64_t grid_words = 0;
+    std::vector<uint32_t> mesh_tri_base;
+    Pool pool;
+    Counters *ctr = nullptr;
+    uint32_t *cancel_dev = nullptr;
+    dl_bake_report report{};
+    uint64_t launches = 0;
+    // last run's results (device)
+    bool have_result = false;
+    uint64_t out_words = 0;
+    std::vector<unsigned long long> mesh_words;
+    uint32_t *words_dev = nullptr;
+    Counters counters{};
+    uint64_t texels = 0;
+    // batched-form graph over the visibility stage, rebuilt when the queue changes
+    cudaGraphExec_t graph = nullptr;
+    uint64_t graph_generation = ~0ull;
+    unsigned long long graph_items = 0;
+    unsigned graph_blocks = 0;
+    ~dl_session() {
+        if (graph) cudaGraphExecDestroy(graph);
+        for (void *p : owned) cudaFree(p);
+        if (stream) cudaStreamDestroy(stream);
+        if (side) cudaStreamDestroy(side);
+    }
+};
+
+namespace dl {
+namespace {
+
+void scan_u32(dl_session &s, const uint32_t *in, uint32_t *out, size_t n) {
+    size_t temp = 0;
+    CK(cub::DeviceScan::ExclusiveSum(nullptr, temp, in, out, n, s.stream));
+    void *tmp = s.pool.get<uint8_t>("scan_tmp", temp);
+    CK(cub::DeviceScan::ExclusiveSum(tmp, temp, in, out, n, s.stream));
+    s.launches += 2;
+}
+void scan_u64(dl_session &s, const unsigned long long *in, unsigned long long *out, size_t n) {
+    size_t temp = 0;
+    CK(cub::DeviceScan::ExclusiveSum(nullptr, temp, in, out, n, s.stream));
+    void *tmp = s.pool.get<uint8_t>("scan_tmp", temp);
+    CK(cub::DeviceScan::ExclusiveSum(tmp, temp, in, out, n, s.stream));
+    s.launches += 2;
+}
+template <class T>
+T read_back(dl_session &s, const T *p) {
+    T v;
+    CK(cudaMemcpyAsync(&v, p, sizeof(T), cudaMemcpyDeviceToHost, s.stream));
+    CK(cudaStreamSynchronize(s.stream));
+    return v;
+}
+unsigned grid_for(size_t n, unsigned block = kBlock) { return (unsigned)((n + block - 1) / block); }
+
+// Blocks the caller until the stream drains, forwarding a cancel request to the device flag.
+void wait(dl_session &s, dl_progress *progress) {
+    bool forwarded = false;
+    for (;;) {
+        cudaError_t q = cudaStreamQuery(s.stream);
+        if (q == cudaSuccess) return;
+        if (q != cudaErrorNotReady) throw CudaError{q, "stream"};
+        if (progress && progress->cancel && !forwarded) {
+            static const uint32_t one = 1;
+            CK(cudaMemcpyAsync(s.cancel_dev, &one, 4, cudaMemcpyHostToDevice, s.side));
+            forwarded = true;
+        }
+        std::this_thread::yield();
+    }
+}
+
+dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bake_config *cfg, dl_session *&out) {
+    auto s = std::make_unique<dl_session>();
+    s->options = *o;
+    if (cfg) s->config = *cfg;
+    std::string err;
+    dl_status st = prepare_scene(*in, *o, s->host, err);
+    if (st != DL_OK) {
+        g_error = err;
+        return st;
+    }
+    HostScene &h = s->host;
+    for (uint32_t r : h.resolution)
+        if (r > 65535) {
+            g_error = "shadow maps larger than 65535 texels per side are not supported";
+            return DL_UNSUPPORTED;
+        }
+    build_bvh(h);
+    // the traversal stack holds one entry per level below the root
+    if (h.bvh_depth >= (uint32_t)kStack) {
+        g_error = "occluder BVH deeper than the traversal stack";
+        return DL_UNSUPPORTED;
+    }
+    s->device = (int)s->config.device;
+    CK(cudaSetDevice(s->device));
+    CK(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device));
+    CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+
+    // flatten meshes
+    uint32_t M = (uint32_t)h.meshes.size();
+    std::vector<uint32_t> vbase(M + 1, 0), ibase(M + 1, 0), tbase(M + 1, 0), flags(M), alpha(M * 4, 0);
+    std::vector<uint64_t> ids(M);
+    std::vector<float> albedo(M * 3);
+    std::vector<uint8_t> alpha_pool;
+    for (uint32_t m = 0; m < M; ++m) {
+        const dl_mesh &mm = *h.meshes[m];
+        vbase[m + 1] = vbase[m] + mm.vertex_count;
+        ibase[m + 1] = ibase[m] + (uint32_t)mm.index_count;
+        tbase[m + 1] = tbase[m] + (uint32_t)(mm.index_count / 3);
+        ids[m] = mm.id;
+        for (int k = 0; k < 3; ++k) albedo[m * 3 + k] = mm.albedo[k];
+        flags[m] = (mm.normals ? kMeshNormals : 0) | (mm.occludes ? kMeshOccludes : 0) |
+                   (mm.alpha && mm.uv0 ? kMeshAlpha : 0);
+        if (mm.alpha && mm.uv0) {
+            alpha[m * 4] = (uint32_t)alpha_pool.size();
+            alpha[m * 4 + 1] = mm.alpha->width;
+            alpha[m * 4 + 2] = mm.alpha->height;
+            std::memcpy(&alpha[m * 4 + 3], &mm.alpha->cutoff, 4);
+            size_t n = (size_t)mm.alpha->width * mm.alpha->height;
+            for (size_t i = 0; i < n; ++i) alpha_pool.push_back(mm.alpha->rgba8[i * 4 + 3]);
+        }
+    }
+    uint32_t V = vbase[M], I = ibase[M], T = tbase[M];
+    std::vector<float> pos(V * 3), nrm(V * 3, 0.0f), uv1(V * 2), uv0(V * 2, 0.0f);
+    std::vector<uint32_t> idx(I), tri_mesh(T);
+    for (uint32_t m = 0; m < M; ++m) {
+        const dl_mesh &mm = *h.meshes[m];
+        std::memcpy(&pos[vbase[m] * 3], mm.positions, mm.vertex_count * 12ull);
+        if (mm.normals) std::memcpy(&nrm[vbase[m] * 3], mm.normals, mm.vertex_count * 12ull);
+        for (uint32_t v = 0; v < mm.vertex_count; ++v) {
+            float a = mm.uv1[v * 2], b = mm.uv1[v * 2 + 1];
+            bool ok = std::isfinite(a) && std::isfinite(b);  // mesh_builder.rs:30-40
+            uv1[(vbase[m] + v) * 2] = ok ? a : 0.0f;
+            uv1[(vbase[m] + v) * 2 + 1] = ok ? b : 0.0f;
+        }
+        if (mm.uv0) std::memcpy(&uv0[vbase[m] * 2], mm.uv0, mm.vertex_count * 8ull);
+        std::memcpy(&idx[ibase[m]], mm.indices, mm.index_count * 4ull);
+        for (uint32_t t = tbase[m]; t < tbase[m + 1]; ++t) tri_mesh[t] = m;
+    }
+    s->grid_off.resize(M + 1);
+    s->grid_words = 0;
+    for (uint32_t m = 0; m < M; ++m) {
+        s->grid_off[m] = s->grid_words;
+        s->grid_words += ((uint64_t)h.resolution[m] * h.resolution[m] + 31) / 32;
+    }
+    s->grid_off[M] = s->grid_words;
+    s->mesh_tri_base = tbase;
+    uint32_t N = (uint32_t)h.occ_mesh.size();
+    std::vector<uint32_t> occ_leaf(N);
+    for (uint32_t k = 0; k < N; ++k) {
+        uint32_t occ;
+        std::memcpy(&occ, &h.tri_v0[k * 4 + 3], 4);
+        occ_leaf[occ] = k;
+    }
+
+    uint64_t &bytes = s->scene_bytes;
+    auto up = [&](const void *src, size_t n, auto *&dst) {
+        using T = std::remove_const_t<std::remove_pointer_t<std::remove_reference_t<decltype(dst)>>>;
+        T *p = dev_alloc<T>(s->owned, n / sizeof(T) + 1, bytes);
+        if (n) CK(cudaMemcpy(p, src, n, cudaMemcpyHostToDevice));
+        dst = p;
+        s->report.h2d_bytes += n;
+    };
+    DevScene &sc = s->sc;
+    up(h.nodes.data(), h.nodes.size() * sizeof(BvhNode), sc.nodes);
+    up(h.tri_v0.data(), h.tri_v0.size() * 4, sc.tri_v0);
+    up(h.tri_e1.data(), h.tri_e1.size() * 4, sc.tri_e1);
+    up(h.tri_e2.data(), h.tri_e2.size() * 4, sc.tri_e2);
+    sc.occluders = N;
+    up(h.occ_mesh.data(), N * 4ull, sc.occ_mesh);
+    up(h.occ_tri.data(), N * 4ull, sc.occ_tri);
+    up(occ_leaf.data(), N * 4ull, sc.occ_leaf);
+    sc.mesh_count = M;
+    up(vbase.data(), vbase.size() * 4, sc.mesh_vertex_base);
+    up(ibase.data(), ibase.size() * 4, sc.mesh_index_base);
+    up(tbase.data(), tbase.size() * 4, sc.mesh_tri_base);
+    up(h.resolution.data(), M * 4ull, sc.mesh_res);
+    up(flags.data(), M * 4ull, sc.mesh_flags);
+    up(ids.data(), M * 8ull, sc.mesh_id);
+    up(albedo.data(), M * 12ull, sc.mesh_albedo);
+    up(alpha.data(), M * 16ull, sc.mesh_alpha);
+    up(alpha_pool.data(), alpha_pool.size(), sc.alpha_pool);
+    up(pos.data(), pos.size() * 4, sc.positions);
+    up(nrm.data(), nrm.size() * 4, sc.normals);
+    up(uv1.data(), uv1.size() * 4, sc.uv1);
+    up(uv0.data(), uv0.size() * 4, sc.uv0);
+    up(idx.data(), idx.size() * 4, sc.indices);
+    sc.triangles = T;
+    up(tri_mesh.data(), T * 4ull, sc.tri_mesh);
+    sc.light_count = (uint32_t)h.lights.size();
+    sc.local_lights = h.local_lights;
+    up(h.lights.data(), h.lights.size() * sizeof(DevLight), sc.lights);
+    sc.seed = o->seed;
+    sc.area_samples = o->area_light_samples;
+    sc.area_min_samples = o->area_light_min_samples;
+    sc.sky_samples = o->sky_samples;
+    sc.colored_bounce = o->colored_bounce;
+    s->ctr = dev_alloc<Counters>(s->owned, 1, bytes);
+    s->cancel_dev = dev_alloc<uint32_t>(s->owned, 1, bytes);
+    s->report.bvh_nodes = h.nodes.size();
+    s->report.occluders = N;
+    out = s.release();
+    return DL_OK;
+}
+
+
+// The device pipeline of one bake. Reads back the sizes it needs between stages; everything
+// else stays on the device until dl_session_result.
+dl_status run(dl_session &s, dl_progress *progress) {
+    DevScene &sc = s.sc;
+    const uint32_t T = sc.triangles, M = sc.mesh_count, L = sc.light_count;
+    Pool &P = s.pool;
+    cudaStream_t st = s.stream;
+    s.launches = 0;
+    s.have_result = false;
+    if (progress && progress->cancel) return DL_CANCELLED;
+    if (progress) {
+        progress->stage = 2;  // BakeStage::Meshes (src/bake/progress.rs:8-16)
+        progress->total = M;
+        progress->done = 0;
+    }
+    auto check_cancel = [&]() { return progress && progress->cancel; };
+    cudaEvent_t e0, e1, v0, v1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventCreate(&v0));
+    CK(cudaEventCreate(&v1));
+    struct EventGuard {
+        cudaEvent_t *e[4];
+        ~EventGuard() {
+            for (auto *x : e) cudaEventDestroy(*x);
+        }
+    } guard{{&e0, &e1, &v0, &v1}};
+    CK(cudaEventRecord(e0, st));
+    CK(cudaMemsetAsync(s.ctr, 0, sizeof(Counters), st));
+    CK(cudaMemsetAsync(s.cancel_dev, 0, 4, st));
+
+    // ---- setup + association
+    float4 *tri_face = P.get<float4>("tri_face", T);
+    uint4 *tri_crop = P.get<uint4>("tri_crop", T);
+    uint32_t *tri_cnt = P.get<uint32_t>("tri_cnt", T + 1);
+    uint32_t *tri_off = P.get<uint32_t>("tri_off", T + 1);
+    CK(cudaMemsetAsync(tri_cnt + T, 0, 4, st));
+    if (T) {
+        k_setup<<<grid_for(T), kBlock, 0, st>>>(sc, tri_face, tri_crop, tri_cnt);
+        ++s.launches;
+    }
+    scan_u32(s, tri_cnt, tri_off, T + 1);
+    const uint32_t pairs = read_back(s, tri_off + T);
+    const size_t entries = (size_t)M * L;
+    uint32_t *pair_light = P.get<uint32_t>("pair_light", pairs);
+    uint32_t *pair_tri = P.get<uint32_t>("pair_tri", pairs);
+    uint32_t *region_rect = P.get<uint32_t>("region_rect", entries * 4);
+    if (entries) {
+        k_fill_u32<<<grid_for(entries * 4), kBlock, 0, st>>>(region_rect, entries * 4, kNoRect, 0u);
+        ++s.launches;
+    }
+    if (T) {
+        k_assoc_fill<<<grid_for(T), kBlock, 0, st>>>(sc, tri_face, tri_crop, tri_off, pair_light, pair_tri,
+                                                     region_rect);
+        ++s.launches;
+    }
+    uint32_t *region_words = P.get<uint32_t>("region_words", entries + 1);
+    uint32_t *region_off = P.get<uint32_t>("region_off", entries + 1);
+    k_region_words<<<grid_for(entries + 1), kBlock, 0, st>>>(region_rect, sc.lights, (uint32_t)entries, L ? L : 1,
+                                                             region_words);
+    ++s.launches;
+    scan_u32(s, region_words, region_off, entries + 1);
+    const uint32_t region_total = read_back(s, region_off + entries);
+    uint32_t *region_pool = P.get<uint32_t>("region_pool", region_total);
+    CK(cudaMemsetAsync(region_pool, 0, region_total * 4ull, st));
+
+    // ---- texels
+    uint64_t *grid_off = P.get<uint64_t>("grid_off", M + 1);
+    CK(cudaMemcpyAsync(grid_off, s.grid_off.data(), (M + 1) * 8ull, cudaMemcpyHostToDevice, st));
+    uint32_t *owned = P.get<uint32_t>("owned", s.grid_words);
+    uint32_t *visited = P.get<uint32_t>("visited", s.grid_words);
+    CK(cudaMemsetAsync(owned, 0, s.grid_words * 4, st));
+    CK(cudaMemsetAsync(visited, 0, s.grid_words * 4, st));
+    uint32_t *cen = P.get<uint32_t>("cen", T + 1);
+    uint32_t *tou = P.get<uint32_t>("tou", T + 1);
+    uint32_t *tex_cnt = P.get<uint32_t>("tex_cnt", T + 1);
+    uint32_t *tex_off = P.get<uint32_t>("tex_off", T + 1);
+    const unsigned warp_grid = grid_for((size_t)T * 32);
+    if (T) {
+        k_texels<0><<<warp_grid, kBlock, 0, st>>>(sc, tri_face, owned, grid_off, cen, nullptr, nullptr, nullptr,
+                                                  nullptr, nullptr);
+        k_texels<1><<<warp_grid, kBlock, 0, st>>>(sc, tri_face, owned, grid_off, tou, nullptr, nullptr, nullptr,
+                                                  nullptr, nullptr);
+        s.launches += 2;
+    }
+    k_add_u32<<<grid_for(T + 1), kBlock, 0, st>>>(cen, tou, tex_cnt, T);
+    ++s.launches;
+    scan_u32(s, tex_cnt, tex_off, T + 1);
+    const uint32_t texels_all = read_back(s, tex_off + T);
+    uint32_t *tex_xy = P.get<uint32_t>("tex_xy", texels_all);
+    float4 *tex_pos = P.get<float4>("tex_pos", texels_all);
+    float4 *tex_nrm = P.get<float4>("tex_nrm", texels_all);
+    uint32_t *tex_tri = P.get<uint32_t>("tex_tri", texels_all);
+    uint8_t *buried = P.get<uint8_t>("buried", texels_all);
+    if (T) {
+        k_texels<2><<<warp_grid, kBlock, 0, st>>>(sc, tri_face, owned, grid_off, nullptr, tex_off, tex_xy, tex_pos,
+                                                  tex_nrm, tex_tri);
+        ++s.launches;
+    }
+    if (texels_all) {
+        k_burial<<<grid_for(texels_all), kBlock, 0, st>>>(sc, texels_all, tex_xy, tex_pos, tex_tri, tri_face, buried,
+                                                          s.ctr);
+        ++s.launches;
+    }
+    uint32_t *ctex_cnt = P.get<uint32_t>("ctex_cnt", T + 1);
+    uint32_t *ctex_off = P.get<uint32_t>("ctex_off", T + 1);
+    CK(cudaMemsetAsync(ctex_cnt + T, 0, 4, st));
+    if (T) {
+        k_unburied<false><<<warp_grid, kBlock, 0, st>>>(T, tex_off, buried, ctex_cnt, nullptr, nullptr, nullptr,
+                                                        nullptr, nullptr, nullptr, nullptr);
+        ++s.launches;
+    }
+    scan_u32(s, ctex_cnt, ctex_off, T + 1);
+    const uint32_t texels = read_back(s, ctex_off + T);
+    uint32_t *ctex_xy = P.get<uint32_t>("ctex_xy", texels);
+    float4 *ctex_pos = P.get<float4>("ctex_pos", texels);
+    float4 *ctex_nrm = P.get<float4>("ctex_nrm", texels);
+    if (T) {
+        k_unburied<true><<<warp_grid, kBlock, 0, st>>>(T, tex_off, buried, nullptr, ctex_off, tex_xy, tex_pos,
+                                                       tex_nrm, ctex_xy, ctex_pos, ctex_nrm);
+        ++s.launches;
+    }
+    s.texels = texels;
+    if (check_cancel()) return DL_CANCELLED;
+
+    // ---- visibility
+    TraceArgs ta{};
+    ta.pair_tri = pair_tri;
+    ta.pair_light = pair_light;
+    ta.ctex_off = ctex_off;
+    ta.ctex_xy = ctex_xy;
+    ta.ctex_pos = ctex_pos;
+    ta.ctex_nrm = ctex_nrm;
+    ta.tri_face = tri_face;
+    ta.grid_off = grid_off;
+    ta.visited = visited;
+    ta.region_rect = region_rect;
+    ta.region_off = region_off;
+    ta.region_pool = region_pool;
+    ta.ctr = s.ctr;
+    ta.cancel = s.cancel_dev;
+    if (s.config.form == DL_FORM_PLAIN) {
+        CK(cudaEventRecord(v0, st));
+        for (uint32_t m = 0; m < M; ++m) {
+            uint32_t first = s.mesh_tri_base[m], count = s.mesh_tri_base[m + 1] - first;
+            if (!count) continue;
+            unsigned blocks = (unsigned)std::min<size_t>(grid_for((size_t)count * 32), (size_t)s.sms * 16);
+            k_trace_plain<<<blocks, kBlock, 0, st>>>(sc, ta, first, count, tri_off);
+            ++s.launches;
+            if (progress) progress->done = m + 1;
+        }
+        CK(cudaEventRecord(v1, st));
+    } else {
+        // queue: pairs ordered sky, soft, hard; item prefix sums over their texel counts
+        uint32_t *order = P.get<uint32_t>("order", pairs + 1);
+        uint32_t *flag = P.get<uint32_t>("flag", pairs + 1);
+        uint32_t *fpos = P.get<uint32_t>("fpos", pairs + 1);
+        uint32_t base = 0;
+        for (uint32_t c = 0; c < 3; ++c) {
+            k_pair_class<<<grid_for(pairs + 1), kBlock, 0, st>>>(sc, pair_light, pairs, c, flag);
+            scan_u32(s, flag, fpos, pairs + 1);
+            k_pair_scatter<<<grid_for(pairs), kBlock, 0, st>>>(flag, fpos, pairs, base, order);
+            s.launches += 2;
+            base += read_back(s, fpos + pairs);
+        }
+        uint32_t *icnt = P.get<uint32_t>("icnt", pairs + 1);
+        uint32_t *item_off = P.get<uint32_t>("item_off", pairs + 1);
+        k_item_counts<<<grid_for(pairs + 1), kBlock, 0, st>>>(order, pair_tri, ctex_off, pairs, icnt);
+        ++s.launches;
+        scan_u32(s, icnt, item_off, pairs + 1);
+        const uint32_t items = read_back(s, item_off + pairs);
+        s.report.work_items = items;
+        unsigned long long *head = P.get<unsigned long long>("head", 1);
+        ta.order = order;
+        ta.item_off = item_off;
+        ta.pairs = pairs;
+        ta.items = items;
+        ta.head = head;
+        ta.grab = s.config.chunk_texels ? std::max(1u, s.config.chunk_texels / 32) : 1;
+        int per_sm = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_batched, kBlock, 0));
+        if (s.config.blocks_per_sm) per_sm = std::min(per_sm, (int)s.config.blocks_per_sm);
+        unsigned blocks = (unsigned)std::max(1, per_sm * s.sms);
+        // The visibility stage runs from a CUDA graph: the memset of the queue head and the
+        // persistent kernel, captured once per queue layout and replayed.
+        if (!s.graph || s.graph_generation != P.generation || s.graph_items != items || s.graph_blocks != blocks) {
+            if (s.graph) cudaGraphExecDestroy(s.graph);
+            s.graph = nullptr;
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            cudaMemsetAsync(head, 0, sizeof(unsigned long long), st);
+            if (items) k_trace_batched<<<blocks, kBlock, 0, st>>>(sc, ta);
+            CK(cudaStreamEndCapture(st, &g));
+            CK(cudaGraphInstantiate(&s.graph, g, 0));
+            cudaGraphDestroy(g);
+            s.graph_generation = P.generation;
+            s.graph_items = items;
+            s.graph_blocks = blocks;
+        }
+        CK(cudaEventRecord(v0, st));
+        CK(cudaGraphLaunch(s.graph, st));
+        if (items) ++s.launches;
+        CK(cudaEventRecord(v1, st));
+    }
+    wait(s, progress);
+    if (check_cancel()) return DL_CANCELLED;
+
+    // ---- optimize, seams
+    uint8_t *keep = P.get<uint8_t>("keep", pairs);
+    uint32_t *kept_cnt = P.get<uint32_t>("kept_cnt", T + 1);
+    uint32_t *entry_off = P.get<uint32_t>("entry_off", T + 1);
+    uint8_t *used = P.get<uint8_t>("used", entries);
+    CK(cudaMemsetAsync(used, 0, entries, st));
+    CK(cudaMemsetAsync(kept_cnt + T, 0, 4, st));
+    if (T) {
+        k_optimize<<<grid_for(T), kBlock, 0, st>>>(sc, tri_off, pair_light, region_rect, region_off, region_pool,
+                                                   nullptr, keep, kept_cnt, used, s.ctr);
+        ++s.launches;
+    }
+    if (entries) {
+        k_pad_seams<<<(unsigned)entries, kBlock, 0, st>>>(sc, used, region_rect, region_off, region_pool, visited,
+                                                          grid_off);
+        ++s.launches;
+    }
+    scan_u32(s, kept_cnt, entry_off, T + 1);
+    const uint32_t kept = read_back(s, entry_off + T);
+
+    // ---- serialize
+    const uint32_t stride = s.host.bounce_in_scene ? 3 : 2;
+    unsigned long long *ld_words = P.get<unsigned long long>("ld_words", T + 1);
+    unsigned long long *pl_words = P.get<unsigned long long>("pl_words", T + 1);
+    unsigned long long *ld_scan = P.get<unsigned long long>("ld_scan", T + 1);
+    unsigned long long *pl_scan = P.get<unsigned long long>("pl_scan", T + 1);
+    k_tri_words<<<grid_for(T + 1), kBlock, 0, st>>>(sc, tri_off, pair_light, keep, tri_crop, stride, ld_words,
+                                                    pl_words);
+    ++s.launches;
+    scan_u64(s, ld_words, ld_scan, T + 1);
+    scan_u64(s, pl_words, pl_scan, T + 1);
+    unsigned long long *mesh_words = P.get<unsigned long long>("mesh_words", M + 1);
+    unsigned long long *mesh_base = P.get<unsigned long long>("mesh_base", M + 1);
+    k_mesh_words<<<grid_for(M + 1), kBlock, 0, st>>>(sc, ld_scan, pl_scan, mesh_words);
+    ++s.launches;
+    scan_u64(s, mesh_words, mesh_base, M + 1);
+    const unsigned long long total_words = read_back(s, mesh_base + M);
+    uint32_t *words = P.get<uint32_t>("words", total_words);
+    uint32_t *entry_pair = P.get<uint32_t>("entry_pair", kept);
+    unsigned long long *entry_dst = P.get<unsigned long long>("entry_dst", kept);
+    if (T) {
+        k_serialize<<<grid_for(T), kBlock, 0, st>>>(sc, tri_off, pair_light, keep, tri_crop, stride, ld_scan, pl_scan,
+                                                    mesh_base, entry_off, words, entry_pair, entry_dst);
+        ++s.launches;
+    }
+    if (kept) {
+        k_crop<<<grid_for((size_t)kept * 32), kBlock, 0, st>>>(sc, kept, entry_pair, entry_dst, pair_tri, pair_light,
+                                                               tri_crop, region_rect, region_off, region_pool, words);
+        ++s.launches;
+    }
+    CK(cudaEventRecord(e1, st));
+    s.mesh_words.resize(M + 1);
+    CK(cudaMemcpyAsync(s.mesh_words.data(), mesh_words, (M + 1) * 8ull, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&s.counters, s.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    float ms = 0.0f, vms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    CK(cudaEventElapsedTime(&vms, v0, v1));
+    s.report.ms_device = ms;
+    s.report.ms_visibility = vms;
+    s.report.pairs = pairs;
+    s.report.shadow_rays = s.counters.rays;
+    s.report.burial_rays = s.counters.burial_rays;
+    s.report.bounce_rays = s.counters.bounce_rays;
+    s.report.photon_rays = s.counters.photon_rays;
+    s.report.kernel_launches = s.launches;
+    s.report.device_bytes = s.scene_bytes + P.bytes;
+    s.out_words = total_words;
+    s.words_dev = words;
+    s.have_result = true;
+    if (progress) {
+        progress->done = M;
+        progress->stage = 4;  // Done
+    }
+    return DL_OK;
+}
+
+// The result in one host allocation: the scene struct, its arrays, then the words.
+struct HostResult {
+    dl_baked_scene scene;
+    std::vector<dl_baked_light> lights;
+    std::vector<dl_light_bvh_node> bvh;
+    std::vector<dl_baked_mesh> meshes;
+    std::vector<uint32_t> words;
+};
+
+dl_status result(dl_session &s, dl_baked_scene *&out) {
+    if (!s.have_result) {
+        g_error = "no finished run in this session";
+        return DL_INVALID_ARGUMENT;
+    }
+    auto r = std::make_unique<HostResult>();
+    const HostScene &h = s.host;
+    r->words.resize(s.out_words);
+    if (s.out_words)
+        CK(cudaMemcpy(r->words.data(), s.words_dev, s.out_words * 4, cudaMemcpyDeviceToHost));
+    s.report.d2h_bytes = s.out_words * 4 + (s.mesh_words.size() * 8) + sizeof(Counters);
+    uint64_t at = 0;
+    for (uint32_t m = 0; m < h.meshes.size(); ++m) {
+        const dl_mesh &mm = *h.meshes[m];
+        dl_baked_mesh b{};
+        b.id = mm.id;
+        b.content_hash = mm.content_hash;
+        b.resolution = h.resolution[m];
+        b.occludes = mm.occludes ? 1 : 0;
+        b.triangles = r->words.data() + at;
+        b.word_count = s.mesh_words[m];
+        at += s.mesh_words[m];
+        r->meshes.push_back(b);
+    }
+    const dl_bake_options &o = s.options;
+    for (size_t i = 0; i < h.light_ptrs.size(); ++i) {
+        const dl_light &l = *h.light_ptrs[i];
+        const DevLight &d = h.lights[i];
+        dl_baked_light b{};
+        b.id = l.id;
+        for (int k = 0; k < 3; ++k) b.origin[k] = l.position[k];
+        b.radius = l.radius;
+        b.shape = l.shape;
+        // the file's shape record (format/lights.rs:27-52): rotation and size only for area/sun
+        bool shaped = l.shape != DL_SHAPE_POINT && l.shape != DL_SHAPE_SKY;
+        b.rotation[0] = shaped ? l.rotation[0] : 0.0f;
+        b.rotation[1] = shaped ? l.rotation[1] : 0.0f;
+        b.rotation[2] = shaped ? l.rotation[2] : 0.0f;
+        b.rotation[3] = shaped ? l.rotation[3] : 1.0f;
+        b.size[0] = shaped ? l.size[0] : 0.0f;
+        b.size[1] = (l.shape == DL_SHAPE_RECTANGLE || l.shape == DL_SHAPE_TUBE) ? l.size[1] : 0.0f;
+        b.bounce_bits = d.bounce_bits;
+        b.shadow_bits_per_texel = d.shadow_bits;
+        r->lights.push_back(b);
+    }
+    r->bvh = h.light_bvh;
+    dl_baked_scene &sc = r->scene;
+    sc = dl_baked_scene{};
+    sc.settings.bounce = h.bounce_in_scene;
+    sc.settings.colored_bounce = h.bounce_in_scene && o.colored_bounce;
+    sc.settings.dynamic_geometry = o.dynamic_geometry;
+    sc.settings.pixel_density = o.pixel_density;
+    sc.settings.max_lightmap_size = o.max_lightmap_size;
+    sc.settings.distance_cube_resolution = 64;
+    sc.light_count = r->lights.size();
+    sc.lights = r->lights.data();
+    sc.light_bvh_count = r->bvh.size();
+    sc.light_bvh = r->bvh.data();
+    sc.mesh_count = r->meshes.size();
+    sc.meshes = r->meshes.data();
+    sc.stats.meshes = (uint32_t)h.meshes.size();
+    sc.stats.triangles = h.triangles;
+    sc.stats.texels = s.texels;
+    sc.stats.rays = s.counters.rays;
+    sc.stats.lights_removed = s.counters.lights_removed;
+    sc.stats.bounce_rays = s.counters.bounce_rays;
+    sc.stats.triangle_words = s.out_words;
+    out = &r.release()->scene;
+    return DL_OK;
+}
+
+}  // namespace
+}  // namespace dl
+
+// ================================ C ABI ====================================================
+
+#define DL_GUARD(body)                                                                \
+    try {                                                                             \
+        body                                                                          \
+    } catch (const CudaError &e) {                                                    \
+        g_error = std::string(e.what) + ": " + cudaGetErrorString(e.code);            \
+        return e.code == cudaErrorMemoryAllocation ? DL_OUT_OF_MEMORY : DL_CUDA_ERROR; \
+    } catch (const std::bad_alloc &) {                                                \
+        g_error = "host allocation failed";                                           \
+        return DL_OUT_OF_MEMORY;                                                      \
+    } catch (...) {                                                                   \
+        g_error = "unexpected failure";                                               \
+        return DL_CUDA_ERROR;                                                         \
+    }
+
+extern "C" {
+
+uint32_t dl_abi_version(void) { return DL_ABI_VERSION; }
+
+const char *dl_status_string(dl_status status) {
+    switch (status) {
+        case DL_OK: return "ok";
+        case DL_CANCELLED: return "cancelled";
+        case DL_DUPLICATE_ID: return "duplicate id";
+        case DL_INVALID_MESH: return "invalid mesh";
+        case DL_INVALID_LIGHT: return "invalid light";
+        case DL_INVALID_OPTIONS: return "invalid options";
+        case DL_CUDA_ERROR: return "cuda error";
+        case DL_OUT_OF_MEMORY: return "out of memory";
+        case DL_QUEUE_TIMEOUT: return "queue timeout";
+        case DL_BUSY: return "busy";
+        case DL_UNSUPPORTED: return "unsupported";
+        case DL_INVALID_ARGUMENT: return "invalid argument";
+    }
+    return "unknown";
+}
+
+const char *dl_last_error(void) { return g_error.c_str(); }
+
+void dl_default_options(dl_bake_options *o) {
+    if (!o) return;
+    *o = dl_bake_options{};
+    o->pixel_density = 128.0f;
+    o->max_lightmap_size = 2048;
+    o->bounce_compression = 8;
+    o->dynamic_geometry = DL_GEOMETRY_ANGULAR;
+    o->skip_bounce = 0;
+    o->photon_cube_resolution = 512;
+    o->area_light_samples = 64;
+    o->area_light_min_samples = 16;
+    o->sun_map_resolution = 2048;
+    o->sky_samples = 64;
+    o->sky_probe_spacing = 1.0f;
+    o->colored_bounce = 0;
+    o->seed = 0;
+}
+
+dl_status dl_session_create(const dl_bake_input *input, const dl_bake_options *options,
+                            const dl_bake_config *config, dl_session **out) {
+    if (!input || !options || !out) {
+        g_error = "null argument";
+        return DL_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    DL_GUARD({
+        dl_session *s = nullptr;
+        auto t0 = std::chrono::steady_clock::now();
+        dl_status st = create(input, options, config, s);
+        if (st != DL_OK) return st;
+        s->report.ms_upload = ms_since(t0);
+        *out = s;
+        return DL_OK;
+    })
+}
+
+dl_status dl_session_run(dl_session *s, dl_progress *progress) {
+    if (!s) {
+        g_error = "null session";
+        return DL_INVALID_ARGUMENT;
+    }
+    DL_GUARD({
+        CK(cudaSetDevice(s->device));
+        return run(*s, progress);
+    })
+}
+
+dl_status dl_session_result(dl_session *s, dl_baked_scene **out) {
+    if (!s || !out) {
+        g_error = "null argument";
+        return DL_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    DL_GUARD({
+        CK(cudaSetDevice(s->device));
+        auto t0 = std::chrono::steady_clock::now();
+        dl_status st = result(*s, *out);
+        s->report.ms_download = ms_since(t0);
+        return st;
+    })
+}
+
+dl_status dl_session_report(const dl_session *s, dl_bake_report *report) {
+    if (!s || !report) return DL_INVALID_ARGUMENT;
+    *report = s->report;
+    return DL_OK;
+}
+
+void dl_session_destroy(dl_session *s) { delete s; }
+
+void dl_baked_scene_free(dl_baked_scene *scene) { delete reinterpret_cast<HostResult *>(scene); }
+
+dl_status dl_bake_ex(const dl_bake_input *input, const dl_bake_options *options, const dl_bake_config *config,
+                     dl_progress *progress, dl_baked_scene **out, dl_bake_report *report) {
+    if (!input || !options || !out) {
+        g_error = "null argument";
+        return DL_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    std::unique_lock<std::mutex> lock(g_busy, std::try_to_lock);
+    if (!lock.owns_lock()) {
+        g_error = "another bake is running in this process";
+        return DL_BUSY;
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    if (progress) {
+        progress->stage = 0;
+        if (progress->cancel) {
+            g_error = "the bake was cancelled";
+            return DL_CANCELLED;
+        }
+    }
+    dl_session *s = nullptr;
+    dl_status st = dl_session_create(input, options, config, &s);
+    if (st != DL_OK) return st;
+    std::unique_ptr<dl_session> owner(s);
+    st = dl_session_run(s, progress);
+    if (st == DL_CANCELLED) g_error = "the bake was cancelled";
+    if (st != DL_OK) return st;
+    st = dl_session_result(s, out);
+    if (report) {
+        *report = s->report;
+        report->ms_total = ms_since(t0);
+    }
+    return st;
+}
+
+dl_status dl_bake(const dl_bake_input *input, const dl_bake_options *options, dl_progress *progress,
+                  dl_baked_scene **out) {
+    dl_bake_config cfg{};
+    return dl_bake_ex(input, options, &cfg, progress, out, nullptr);
+}
+
+dl_status dl_encode_payload(const dl_baked_scene *scene, uint8_t **bytes, uint64_t *length, uint32_t *crc) {
+    if (!scene || !bytes || !length) return DL_INVALID_ARGUMENT;
+    try {
+        std::vector<uint8_t> p = encode_payload(*scene);
+        uint8_t *b = static_cast<uint8_t *>(std::malloc(p.size() ? p.size() : 1));
+        if (!b) return DL_OUT_OF_MEMORY;
+        if (!p.empty()) std::memcpy(b, p.data(), p.size());
+        *bytes = b;
+        *length = p.size();
+        if (crc) *crc = crc32_ieee(p.data(), p.size());
+        return DL_OK;
+    } catch (...) {
+        return DL_OUT_OF_MEMORY;
+    }
+}
+
+void dl_free(void *p) { std::free(p); }
+
+}  // extern "C"

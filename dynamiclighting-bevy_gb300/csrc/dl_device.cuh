@@ -1,0 +1,202 @@
+// Device side of the bake: the resident scene, the ray queries and per-texel visibility.
+//
+// Ray queries restate the reference's Occluders (src/bake/occluder.rs:171-251): two-sided
+// Möller–Trumbore with hits for 0 <= t <= max, any-hit for shadow rays, closest-hit with ties
+// going to the lowest occluder index, optional alpha test. The BVH only prunes: node boxes are
+// padded and the slab test keeps a relative slack, so no triangle the exact test would report is
+// ever culled and results equal a scan over every occluder.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "dl_host.hpp"
+#include "dl_math.cuh"
+
+namespace dl {
+
+// Everything the kernels read, as device pointers (one struct passed by value).
+struct DevScene {
+    // BVH and triangles in leaf order
+    const float4 *nodes;  // 4 float4 per node
+    const float4 *tri_v0, *tri_e1, *tri_e2;
+    uint32_t occluders;
+    // occluder index -> mesh, triangle in mesh, position in leaf order
+    const uint32_t *occ_mesh, *occ_tri, *occ_leaf;
+    // meshes (sorted order)
+    uint32_t mesh_count;
+    const uint32_t *mesh_vertex_base, *mesh_index_base, *mesh_tri_base, *mesh_res;
+    const uint32_t *mesh_flags;  // kMesh* bits
+    const uint64_t *mesh_id;
+    const float *mesh_albedo;     // 3 per mesh
+    const uint32_t *mesh_alpha;   // 4 per mesh: byte offset, width, height, cutoff bits
+    const uint8_t *alpha_pool;
+    // vertex data (global vertex index = base + local)
+    const float *positions, *normals, *uv1, *uv0;  // 3, 3, 2, 2 per vertex
+    const uint32_t *indices;                       // local vertex indices
+    // triangles
+    uint32_t triangles;
+    const uint32_t *tri_mesh;
+    // lights in slot order
+    uint32_t light_count, local_lights;
+    const DevLight *lights;
+    // options
+    uint64_t seed;
+    uint32_t area_samples, area_min_samples, sky_samples;
+    uint32_t colored_bounce;
+};
+enum : uint32_t { kMeshNormals = 1, kMeshOccludes = 2, kMeshAlpha = 4 };
+
+__device__ __forceinline__ float4 ldg4(const float4 *p) { return __ldg(p); }
+
+// AlphaTexture::is_opaque (src/bake/input.rs:79-97) at the hit's interpolated UV0.
+__device__ __forceinline__ uint32_t wrap_texel(float coordinate, uint32_t size) {
+    float r = fmodf(coordinate, 1.0f);
+    if (r < 0.0f) r = r + 1.0f;
+    float t = floorf(r * (float)size);
+    if (isfinite(t)) {
+        uint32_t u = f2u(t);
+        return u < size - 1 ? u : size - 1;
+    }
+    return 0;
+}
+__device__ __noinline__ bool alpha_blocks(const DevScene &sc, uint32_t occ, float u, float v) {
+    uint32_t m = sc.occ_mesh[occ];
+    if (!(sc.mesh_flags[m] & kMeshAlpha)) return true;
+    const uint32_t *tex = sc.mesh_alpha + m * 4;
+    uint32_t width = tex[1], height = tex[2];
+    if (width == 0 || height == 0) return true;
+    const uint32_t *c = sc.indices + sc.mesh_index_base[m] + (size_t)sc.occ_tri[occ] * 3;
+    uint32_t vb = sc.mesh_vertex_base[m];
+    float wx = 1.0f - u - v;
+    const float *a = sc.uv0 + (size_t)(vb + c[0]) * 2, *b = sc.uv0 + (size_t)(vb + c[1]) * 2,
+                *d = sc.uv0 + (size_t)(vb + c[2]) * 2;
+    float uvx = a[0] * wx + b[0] * u + d[0] * v;
+    float uvy = a[1] * wx + b[1] * u + d[1] * v;
+    uint32_t x = wrap_texel(uvx, width), y = wrap_texel(uvy, height);
+    uint8_t alpha = sc.alpha_pool[tex[0] + (size_t)y * width + x];
+    return (float)alpha / 255.0f >= __uint_as_float(tex[3]);
+}
+
+// intersect (occluder.rs:225-251) on a triangle stored as v0, e1 = v1 - v0, e2 = v2 - v0.
+__device__ __forceinline__ bool tri_test(float4 v0, float4 e1v, float4 e2v, f3 o, f3 d, float max, float &t,
+                                         float &u, float &v) {
+    f3 e1{e1v.x, e1v.y, e1v.z}, e2{e2v.x, e2v.y, e2v.z};
+    f3 p = cross(d, e2);
+    float det = dot(e1, p);
+    if (det == 0.0f || !isfinite(det)) return false;
+    float inv = 1.0f / det;
+    f3 s{o.x - v0.x, o.y - v0.y, o.z - v0.z};
+    u = dot(s, p) * inv;
+    if (!(u >= 0.0f && u <= 1.0f)) return false;
+    f3 q = cross(s, e1);
+    v = dot(d, q) * inv;
+    if (v < 0.0f || u + v > 1.0f) return false;
+    t = dot(e2, q) * inv;
+    return t >= 0.0f && t <= max;
+}
+
+struct Hit {
+    float t, u, v;
+    uint32_t occluder;
+};
+
+constexpr int kStack = 64;  // >= BVH depth; the host refuses deeper trees
+
+// Slab test of both children of a node against the ray [0, tmax]. Boxes are padded on the host
+// and the exit distance gets a relative slack, so the test only ever errs towards visiting.
+__device__ __forceinline__ void box2(const float4 &a, const float4 &b, const float4 &c, f3 inv, f3 oinv, float tmax,
+                                     bool &h0, bool &h1, float &n0, float &n1) {
+    float lx0 = __fmaf_rn(a.x, inv.x, -oinv.x), hx0 = __fmaf_rn(a.y, inv.x, -oinv.x);
+    float ly0 = __fmaf_rn(a.z, inv.y, -oinv.y), hy0 = __fmaf_rn(a.w, inv.y, -oinv.y);
+    float lz0 = __fmaf_rn(c.x, inv.z, -oinv.z), hz0 = __fmaf_rn(c.y, inv.z, -oinv.z);
+    float lx1 = __fmaf_rn(b.x, inv.x, -oinv.x), hx1 = __fmaf_rn(b.y, inv.x, -oinv.x);
+    float ly1 = __fmaf_rn(b.z, inv.y, -oinv.y), hy1 = __fmaf_rn(b.w, inv.y, -oinv.y);
+    float lz1 = __fmaf_rn(c.z, inv.z, -oinv.z), hz1 = __fmaf_rn(c.w, inv.z, -oinv.z);
+    float en0 = fmaxf(fmaxf(fminf(lx0, hx0), fminf(ly0, hy0)), fmaxf(fminf(lz0, hz0), 0.0f));
+    float ex0 = fminf(fminf(fmaxf(lx0, hx0), fmaxf(ly0, hy0)), fminf(fmaxf(lz0, hz0), tmax));
+    float en1 = fmaxf(fmaxf(fminf(lx1, hx1), fminf(ly1, hy1)), fmaxf(fminf(lz1, hz1), 0.0f));
+    float ex1 = fminf(fminf(fmaxf(lx1, hx1), fmaxf(ly1, hy1)), fminf(fmaxf(lz1, hz1), tmax));
+    const float slack = 1.0f + 2.0e-6f;
+    h0 = en0 <= ex0 * slack;
+    h1 = en1 <= ex1 * slack;
+    n0 = en0;
+    n1 = en1;
+}
+
+__device__ __forceinline__ f3 safe_inv(f3 d) {
+    return f3{1.0f / (d.x == 0.0f ? copysignf(1e-30f, d.x) : d.x), 1.0f / (d.y == 0.0f ? copysignf(1e-30f, d.y) : d.y),
+              1.0f / (d.z == 0.0f ? copysignf(1e-30f, d.z) : d.z)};
+}
+
+// Any-hit (ANY) or closest-hit traversal of the BVH2. Child references: >= 0 an inner node,
+// < 0 a leaf ~(first << 3 | count). `stack` points at this thread's first stack slot in shared
+// memory, slots `stride` apart. For closest-hit, `hit` gets the nearest t (ties to the lowest
+// occluder index, as occluder.rs:205-210) and that test's barycentrics, which equal the ones
+// the reference recomputes with max = infinity.
+template <bool ANY>
+__device__ bool traverse(const DevScene &sc, f3 o, f3 dir, float max, bool alpha, int *stack, int stride, Hit &hit) {
+    hit.t = INFINITY;
+    hit.u = hit.v = 0.0f;
+    hit.occluder = 0xFFFFFFFFu;
+    if (sc.occluders == 0) return false;
+    f3 d{dir.x + 0.0f, dir.y + 0.0f, dir.z + 0.0f};  // -0 -> +0 (occluder.rs:171-178)
+    f3 inv = safe_inv(d);
+    f3 oinv{o.x * inv.x, o.y * inv.y, o.z * inv.z};
+    float tmax = fmaxf(max, 0.0f);
+    bool found = false;
+    int sp = 0;
+    int ref = 0;
+    for (;;) {
+        if (ref >= 0) {
+            const float4 *nd = sc.nodes + (size_t)ref * 4;
+            float4 a = ldg4(nd), b = ldg4(nd + 1), c = ldg4(nd + 2), r = ldg4(nd + 3);
+            bool h0, h1;
+            float n0, n1;
+            box2(a, b, c, inv, oinv, ANY ? tmax : fminf(tmax, hit.t), h0, h1, n0, n1);
+            int r0 = __float_as_int(r.x), r1 = __float_as_int(r.y);
+            h0 = h0 && r0 != -1;  // ~0: an empty leaf
+            h1 = h1 && r1 != -1;
+            if (h0 && h1) {
+                bool swap = n1 < n0;
+                stack[sp * stride] = swap ? r0 : r1;
+                ++sp;
+                ref = swap ? r1 : r0;
+                continue;
+            }
+            if (h0 || h1) {
+                ref = h0 ? r0 : r1;
+                continue;
+            }
+        } else {
+            uint32_t packed = (uint32_t)(~ref);
+            uint32_t first = packed >> 3, count = packed & 7u;
+            for (uint32_t k = 0; k < count; ++k) {
+                uint32_t i = first + k;
+                float4 v0 = ldg4(sc.tri_v0 + i);
+                float t, u, v;
+                if (!tri_test(v0, ldg4(sc.tri_e1 + i), ldg4(sc.tri_e2 + i), o, d, max, t, u, v)) continue;
+                uint32_t occ = __float_as_uint(v0.w);
+                if (alpha && !alpha_blocks(sc, occ, u, v)) continue;
+                if (ANY) return true;
+                if (isfinite(t) && (t < hit.t || (t == hit.t && occ < hit.occluder))) {
+                    found = true;
+                    hit.t = t;
+                    hit.u = u;
+                    hit.v = v;
+                    hit.occluder = occ;
+                }
+            }
+        }
+        if (sp == 0) return found;
+        --sp;
+        ref = stack[sp * stride];
+    }
+}
+
+__device__ __forceinline__ bool occluded(const DevScene &sc, f3 o, f3 d, float max, bool alpha, int *stack,
+                                         int stride) {
+    Hit h;
+    return traverse<true>(sc, o, d, max, alpha, stack, stride, h);
+}
+
+}  // namespace dl

@@ -1,0 +1,582 @@
+// Host half of the bake (see dl_host.hpp). Compiled with -ffp-contract=off: the f32 formulas
+// here (surface areas, light bounds, light frames) must round like the reference's Rust.
+#include "dl_host.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <future>
+#include <numeric>
+
+namespace dl {
+
+namespace {
+
+std::string hex_id(uint64_t id) {
+    char b[32];
+    std::snprintf(b, sizeof b, "%#018llx", (unsigned long long)id);
+    return b;
+}
+
+// BakeOptions::validate (src/bake/input.rs:336-373)
+bool check_options(const dl_bake_options &o, std::string &err) {
+    const char *bad = nullptr;
+    if (!(std::isfinite(o.pixel_density) && o.pixel_density > 0.0f)) bad = "pixel density must be positive";
+    else if (o.max_lightmap_size < 2) bad = "the maximum shadow map size must be at least 2";
+    else if (o.photon_cube_resolution == 0) bad = "the photon cube resolution must be positive";
+    else if (o.area_light_samples == 0) bad = "area lights need at least one sample";
+    else if (o.sun_map_resolution < 1 || o.sun_map_resolution > 8192) bad = "the sun map resolution must be 1 to 8192";
+    else if (o.sky_samples == 0) bad = "skies need at least one sample";
+    else if (!(std::isfinite(o.sky_probe_spacing) && o.sky_probe_spacing > 0.0f)) bad = "the sky probe spacing must be positive";
+    else if (o.bounce_compression != 8 && o.bounce_compression != 6 && o.bounce_compression != 5 && o.bounce_compression != 4)
+        bad = "bounce compression must be 8, 6, 5 or 4 bits";
+    if (bad) err = std::string("invalid bake options: ") + bad;
+    return bad == nullptr;
+}
+
+// BakeMesh::validate (src/bake/input.rs:233-287)
+bool check_mesh(const dl_mesh &m, std::string &err) {
+    auto bad = [&](const std::string &r) {
+        err = "mesh " + hex_id(m.id) + ": " + r;
+        return false;
+    };
+    if (m.index_count % 3) return bad(std::to_string(m.index_count) + " indices is not a multiple of 3");
+    if (m.index_count && !m.indices) return bad("missing indices");
+    for (uint64_t i = 0; i < m.index_count; ++i)
+        if (m.indices[i] >= m.vertex_count)
+            return bad("index " + std::to_string(m.indices[i]) + " is out of range for " +
+                       std::to_string(m.vertex_count) + " vertices");
+    if (m.vertex_count && (!m.positions || !m.uv1)) return bad("missing positions or UV1 coordinates");
+    for (uint64_t i = 0; i < (uint64_t)m.vertex_count * 3; ++i)
+        if (!std::isfinite(m.positions[i])) return bad("non-finite vertex position");
+    if (m.alpha) {
+        if (!m.uv0) return bad("an alpha texture needs UV0");
+        if ((uint64_t)m.alpha->width * m.alpha->height && !m.alpha->rgba8)
+            return bad("alpha texture size doesn't match its data");
+    }
+    return true;
+}
+
+bool unit_quat(const float q[4]) {
+    for (int i = 0; i < 4; ++i)
+        if (!std::isfinite(q[i])) return false;
+    float n = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+    return std::fabs(n - 1.0f) <= 2e-4f;
+}
+
+// BakeLight::validate (src/bake/input.rs:290-323)
+bool check_light(const dl_light &l, std::string &err) {
+    auto bad = [&](const char *r) {
+        err = "light " + hex_id(l.id) + ": " + r;
+        return false;
+    };
+    for (int i = 0; i < 3; ++i)
+        if (!std::isfinite(l.position[i])) return bad("non-finite position");
+    if (l.shape > DL_SHAPE_SKY) return bad("unknown light shape");
+    bool distant = l.shape == DL_SHAPE_SUN || l.shape == DL_SHAPE_SKY;
+    if (!distant && !(std::isfinite(l.radius) && l.radius > 0.0f)) return bad("radius must be positive and finite");
+    if (l.shape == DL_SHAPE_RECTANGLE || l.shape == DL_SHAPE_TUBE) {
+        if (!std::isfinite(l.size[0]) || !std::isfinite(l.size[1]) || l.size[0] < 0.0f || l.size[1] < 0.0f)
+            return bad("area light size must be finite and not negative");
+        if (!unit_quat(l.rotation)) return bad("area light rotation must be a unit quaternion");
+    }
+    if (l.shape == DL_SHAPE_SUN) {
+        if (!unit_quat(l.rotation)) return bad("sun rotation must be a unit quaternion");
+        if (!(l.size[0] >= 0.0f && l.size[0] <= 10.0f)) return bad("sun angular diameter must be 0 to 10 degrees");
+    }
+    if (l.bounce_compression >= 0 && l.bounce_compression != 8 && l.bounce_compression != 6 &&
+        l.bounce_compression != 5 && l.bounce_compression != 4)
+        return bad("bounce compression must be 8, 6, 5 or 4 bits");
+    return true;
+}
+
+// ---- light BVH (src/bake/light_bvh.rs:59-189): SAH over light positions, <= 2 per leaf ------
+struct Box3 {
+    f3 lo{INFINITY, INFINITY, INFINITY}, hi{-INFINITY, -INFINITY, -INFINITY};
+    void add(const Box3 &b) {
+        lo = vmin(lo, b.lo);
+        hi = vmax(hi, b.hi);
+    }
+    // Aabb::half_area_x2 (src/bake/geometry.rs:49-55)
+    float area2() const {
+        f3 e = sub(hi, lo);
+        if (fminf(fminf(e.x, e.y), e.z) < 0.0f) return 0.0f;
+        return 2.0f * (e.x * e.y + e.y * e.z + e.z * e.x);
+    }
+};
+Box3 sphere_box(f3 c, float r) { return Box3{sub(c, f3{r, r, r}), add(c, f3{r, r, r})}; }
+float axis_of(f3 v, int a) { return a == 0 ? v.x : a == 1 ? v.y : v.z; }
+
+struct LightBvhBuild {
+    const std::vector<f3> &pos;
+    const std::vector<float> &rad;
+    std::vector<uint32_t> order;
+    std::vector<dl_light_bvh_node> nodes;
+
+    void bounds(size_t n) {
+        Box3 b;
+        for (uint32_t k = nodes[n].left_first; k < nodes[n].left_first + nodes[n].count; ++k)
+            b.add(sphere_box(pos[order[k]], rad[order[k]]));
+        nodes[n].aabb_min[0] = b.lo.x; nodes[n].aabb_min[1] = b.lo.y; nodes[n].aabb_min[2] = b.lo.z;
+        nodes[n].aabb_max[0] = b.hi.x; nodes[n].aabb_max[1] = b.hi.y; nodes[n].aabb_max[2] = b.hi.z;
+    }
+    float cost(uint32_t first, uint32_t count, int ax, float split) const {
+        Box3 l, r;
+        uint32_t nl = 0, nr = 0;
+        for (uint32_t k = first; k < first + count; ++k) {
+            uint32_t i = order[k];
+            if (axis_of(pos[i], ax) < split) { ++nl; l.add(sphere_box(pos[i], rad[i])); }
+            else { ++nr; r.add(sphere_box(pos[i], rad[i])); }
+        }
+        if (!nl || !nr) return 3.40282347e+38f;
+        return (float)nl * l.area2() + (float)nr * r.area2();
+    }
+    void split(size_t n) {
+        uint32_t first = nodes[n].left_first, count = nodes[n].count;
+        if (count <= 2) return;
+        Box3 box{f3{nodes[n].aabb_min[0], nodes[n].aabb_min[1], nodes[n].aabb_min[2]},
+                 f3{nodes[n].aabb_max[0], nodes[n].aabb_max[1], nodes[n].aabb_max[2]}};
+        float parent = (float)count * box.area2();
+        bool found = false;
+        int bax = 0;
+        float bsplit = 0.0f, bcost = 3.40282347e+38f;
+        for (int ax = 0; ax < 3; ++ax)
+            for (uint32_t k = 0; k < count; ++k) {
+                float cand = axis_of(pos[order[first + k]], ax);
+                float c = cost(first, count, ax, cand);
+                if (c < bcost) { bcost = c; bax = ax; bsplit = cand; found = true; }
+            }
+        if (!found || bcost >= parent) return;
+        int64_t i = first, j = (int64_t)first + count - 1;
+        while (i <= j) {
+            if (axis_of(pos[order[(size_t)i]], bax) < bsplit) ++i;
+            else { std::swap(order[(size_t)i], order[(size_t)j]); --j; }
+        }
+        uint32_t left_count = (uint32_t)(i - first);
+        if (left_count == 0 || left_count == count) return;
+        size_t left = nodes.size();
+        dl_light_bvh_node a{}, b{};
+        a.left_first = first; a.count = left_count;
+        b.left_first = (uint32_t)i; b.count = count - left_count;
+        nodes.push_back(a);
+        nodes.push_back(b);
+        nodes[n].left_first = (uint32_t)left;
+        nodes[n].count = 0;
+        bounds(left);
+        bounds(left + 1);
+        split(left);
+        split(left + 1);
+    }
+};
+
+}  // namespace
+
+dl_status prepare_scene(const dl_bake_input &in, const dl_bake_options &o, HostScene &s, std::string &err) {
+    if (!check_options(o, err)) return DL_INVALID_OPTIONS;
+    if (o.dynamic_geometry != DL_GEOMETRY_LIGHTING_ONLY) {
+        err = "distance cubes, sun maps and sky probes are not baked by this library: use LightingOnly";
+        return DL_UNSUPPORTED;
+    }
+    if ((in.mesh_count && !in.meshes) || (in.light_count && !in.lights)) {
+        err = "null mesh or light array";
+        return DL_INVALID_ARGUMENT;
+    }
+    // sorted_meshes / sorted_lights (src/bake/baker.rs:205-233)
+    for (uint64_t i = 0; i < in.mesh_count; ++i) s.meshes.push_back(&in.meshes[i]);
+    std::stable_sort(s.meshes.begin(), s.meshes.end(), [](auto *a, auto *b) { return a->id < b->id; });
+    for (size_t i = 1; i < s.meshes.size(); ++i)
+        if (s.meshes[i]->id == s.meshes[i - 1]->id) {
+            err = "two meshes share BakeId " + hex_id(s.meshes[i]->id);
+            return DL_DUPLICATE_ID;
+        }
+    for (auto *m : s.meshes)
+        if (!check_mesh(*m, err)) return DL_INVALID_MESH;
+    std::vector<const dl_light *> lights;
+    for (uint64_t i = 0; i < in.light_count; ++i) lights.push_back(&in.lights[i]);
+    std::stable_sort(lights.begin(), lights.end(), [](auto *a, auto *b) { return a->id < b->id; });
+    for (size_t i = 1; i < lights.size(); ++i)
+        if (lights[i]->id == lights[i - 1]->id) {
+            err = "two lights share BakeId " + hex_id(lights[i]->id);
+            return DL_DUPLICATE_ID;
+        }
+    for (auto *l : lights)
+        if (!check_light(*l, err)) return DL_INVALID_LIGHT;
+
+    // slot order: light BVH order, then suns, then skies (baker.rs:36-50)
+    std::vector<const dl_light *> local, suns, skies;
+    for (auto *l : lights)
+        (l->shape == DL_SHAPE_SUN ? suns : l->shape == DL_SHAPE_SKY ? skies : local).push_back(l);
+    std::vector<f3> pos;
+    std::vector<float> rad;
+    for (auto *l : local) {
+        pos.push_back(f3{l->position[0], l->position[1], l->position[2]});
+        rad.push_back(l->radius);
+    }
+    if (!local.empty()) {
+        LightBvhBuild b{pos, rad, {}, {}};
+        b.order.resize(local.size());
+        std::iota(b.order.begin(), b.order.end(), 0u);
+        dl_light_bvh_node root{};
+        root.count = (uint32_t)local.size();
+        b.nodes.push_back(root);
+        b.bounds(0);
+        b.split(0);
+        s.light_bvh = b.nodes;
+        for (uint32_t i : b.order) s.light_ptrs.push_back(local[i]);
+    }
+    s.local_lights = (uint32_t)s.light_ptrs.size();
+    for (auto *l : suns) s.light_ptrs.push_back(l);
+    for (auto *l : skies) s.light_ptrs.push_back(l);
+
+    for (auto *lp : s.light_ptrs) {
+        const dl_light &l = *lp;
+        DevLight d{};
+        d.position = f3{l.position[0], l.position[1], l.position[2]};
+        d.radius = l.radius;
+        d.shape = l.shape;
+        d.id = l.id;
+        bool distant = l.shape == DL_SHAPE_SUN || l.shape == DL_SHAPE_SKY;
+        bool area = l.shape == DL_SHAPE_RECTANGLE || l.shape == DL_SHAPE_TUBE;
+        bool bounce = l.illumination == DL_ILLUMINATION_SINGLE_BOUNCE && !o.skip_bounce && l.shape != DL_SHAPE_SKY;
+        d.flags = (distant ? kLightDistant : 0) | (l.transparency != DL_TRANSPARENCY_DISABLED ? kLightAlpha : 0) |
+                  (bounce ? kLightBounce : 0) | (l.shape == DL_SHAPE_RECTANGLE ? kLightRect : 0) |
+                  (area ? kLightArea : 0);
+        // shadow_bits_per_texel (light_shape.rs:33-43)
+        d.shadow_bits = l.shape == DL_SHAPE_POINT ? 1
+                        : area ? 4
+                        : l.shape == DL_SHAPE_SUN ? (l.size[0] > 0.0f ? 4 : 1)
+                        : 8;
+        d.bounce_samples = l.bounce_samples < 2 ? 2 : l.bounce_samples;
+        d.bounce_intensity = l.bounce_intensity;
+        d.bounce_bits = bounce ? (l.bounce_compression >= 0 ? (uint32_t)l.bounce_compression : o.bounce_compression) : 0;
+        if (area) {
+            // AreaLightShape::at (src/light/area.rs:48-57) and shape_reach (light_shape.rs:22-28)
+            d.ax = quat_rotate(l.rotation, f3{1.0f, 0.0f, 0.0f});
+            d.ay = quat_rotate(l.rotation, f3{0.0f, 1.0f, 0.0f});
+            d.forward = quat_rotate(l.rotation, f3{0.0f, 0.0f, -1.0f});
+            d.half_x = l.size[0] * 0.5f;
+            d.half_y = l.size[1] * 0.5f;
+            d.reach = l.radius - sqrtf(d.half_x * d.half_x + d.half_y * d.half_y);
+        } else {
+            d.reach = l.radius;
+        }
+        if (l.shape == DL_SHAPE_SUN) {
+            // SunDisk::toward / angular_radius (src/light/shape.rs:95-102)
+            d.toward = normalize(quat_rotate(l.rotation, f3{0.0f, 0.0f, 1.0f}));
+            d.angular_radius = (l.size[0] * 0.5f) * (kPiF / 180.0f);
+            d.tan_radius = tan_f(d.angular_radius);
+            d.sin_radius = sin_f(d.angular_radius);
+        }
+        Box3 b = sphere_box(d.position, d.radius);
+        d.bounds_lo = b.lo;
+        d.bounds_hi = b.hi;
+        s.lights.push_back(d);
+        s.bounce_in_scene |= bounce;
+    }
+    if (s.bounce_in_scene) {
+        err = "one-bounce lighting is not baked by this build of the library";
+        return DL_UNSUPPORTED;
+    }
+
+    // PreparedMesh resolution (mesh_builder.rs:21-51, geometry.rs:66-70) and the occluders
+    // (occluder.rs:80-97)
+    for (uint32_t mi = 0; mi < s.meshes.size(); ++mi) {
+        const dl_mesh &m = *s.meshes[mi];
+        float area = 0.0f;
+        uint64_t tris = m.index_count / 3;
+        s.triangles += tris;
+        for (uint64_t t = 0; t < tris; ++t) {
+            f3 v[3];
+            for (int k = 0; k < 3; ++k) {
+                const float *p = m.positions + (size_t)m.indices[t * 3 + k] * 3;
+                v[k] = f3{p[0], p[1], p[2]};
+            }
+            f3 n = cross(sub(v[1], v[0]), sub(v[2], v[0]));
+            area += length(n) * 0.5f;
+            if (m.occludes && length_sq(n) > 0.0f && std::isfinite(n.x) && std::isfinite(n.y) && std::isfinite(n.z)) {
+                s.occ_mesh.push_back(mi);
+                s.occ_tri.push_back((uint32_t)t);
+            }
+        }
+        float size = ceilf(sqrtf(o.pixel_density * o.pixel_density * area));
+        if (std::isnan(size)) size = 0.0f;
+        uint32_t r = f2u(fminf(size, (float)o.max_lightmap_size));
+        uint32_t hi = std::max(o.max_lightmap_size, 2u);
+        s.resolution.push_back(std::min(std::max(r, 2u), hi));
+    }
+    return DL_OK;
+}
+
+// ---- occluder BVH: binned SAH --------------------------------------------------------------------
+namespace {
+
+struct Prim {
+    float lo[3], hi[3], c[3];
+};
+struct Ref {
+    int32_t ref;
+    uint32_t count;
+    float lo[3], hi[3];
+};
+constexpr int kBins = 16;
+constexpr uint32_t kMaxLeaf = 4;
+constexpr uint32_t kMaxDepth = 60;
+
+struct Builder {
+    std::vector<Prim> prims;
+    std::vector<uint32_t> idx;
+    std::vector<BvhNode> nodes;
+    uint32_t max_depth = 0;
+
+    static float half_area(const float lo[3], const float hi[3]) {
+        float e0 = hi[0] - lo[0], e1 = hi[1] - lo[1], e2 = hi[2] - lo[2];
+        if (e0 < 0 || e1 < 0 || e2 < 0) return 0.0f;
+        return e0 * e1 + e1 * e2 + e2 * e0;
+    }
+
+    // Leaves are referenced as ~(first << 3 | count), count <= 7.
+    Ref leaf(uint32_t first, uint32_t count, const float lo[3], const float hi[3]) {
+        Ref r{~(int32_t)((first << 3) | count), count, {lo[0], lo[1], lo[2]}, {hi[0], hi[1], hi[2]}};
+        return r;
+    }
+
+    Ref build(uint32_t first, uint32_t count, uint32_t depth) {
+        max_depth = std::max(max_depth, depth);
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (uint32_t k = first; k < first + count; ++k) {
+            const Prim &p = prims[idx[k]];
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = std::min(lo[a], p.lo[a]);
+                hi[a] = std::max(hi[a], p.hi[a]);
+                clo[a] = std::min(clo[a], p.c[a]);
+                chi[a] = std::max(chi[a], p.c[a]);
+            }
+        }
+        if (count <= 2 || (depth >= kMaxDepth && count <= 7)) return leaf(first, count, lo, hi);
+        // SAH over kBins bins per axis
+        float best_cost = INFINITY;
+        int best_axis = -1, best_bin = 0;
+        for (int a = 0; a < 3; ++a) {
+            float ext = chi[a] - clo[a];
+            if (!(ext > 0.0f)) continue;
+            float bl[kBins][3], bh[kBins][3];
+            uint32_t bc[kBins] = {};
+            for (int b = 0; b < kBins; ++b)
+                for (int j = 0; j < 3; ++j) { bl[b][j] = INFINITY; bh[b][j] = -INFINITY; }
+            float k = (float)kBins / ext;
+            for (uint32_t i = first; i < first + count; ++i) {
+                const Prim &p = prims[idx[i]];
+                int b = std::min(kBins - 1, (int)((p.c[a] - clo[a]) * k));
+                ++bc[b];
+                for (int j = 0; j < 3; ++j) { bl[b][j] = std::min(bl[b][j], p.lo[j]); bh[b][j] = std::max(bh[b][j], p.hi[j]); }
+            }
+            float rarea[kBins];
+            uint32_t rcount[kBins];
+            float rl[3] = {INFINITY, INFINITY, INFINITY}, rh[3] = {-INFINITY, -INFINITY, -INFINITY};
+            uint32_t rc = 0;
+            for (int b = kBins - 1; b > 0; --b) {
+                rc += bc[b];
+                for (int j = 0; j < 3; ++j) { rl[j] = std::min(rl[j], bl[b][j]); rh[j] = std::max(rh[j], bh[b][j]); }
+                rarea[b] = half_area(rl, rh);
+                rcount[b] = rc;
+            }
+            float ll[3] = {INFINITY, INFINITY, INFINITY}, lh[3] = {-INFINITY, -INFINITY, -INFINITY};
+            uint32_t lc = 0;
+            for (int b = 0; b < kBins - 1; ++b) {
+                lc += bc[b];
+                for (int j = 0; j < 3; ++j) { ll[j] = std::min(ll[j], bl[b][j]); lh[j] = std::max(lh[j], bh[b][j]); }
+                if (!lc || !rcount[b + 1]) continue;
+                float c = half_area(ll, lh) * (float)lc + rarea[b + 1] * (float)rcount[b + 1];
+                if (c < best_cost) { best_cost = c; best_axis = a; best_bin = b; }
+            }
+        }
+        float parent_area = half_area(lo, hi);
+        float leaf_cost = (float)count;
+        float split_cost = 0.3f + (parent_area > 0.0f ? best_cost / parent_area : (float)count);
+        uint32_t mid;
+        if (best_axis < 0 || depth >= kMaxDepth) {
+            if (count <= kMaxLeaf) return leaf(first, count, lo, hi);
+            mid = first + count / 2;  // coincident centroids: split by index
+        } else {
+            if (count <= kMaxLeaf && leaf_cost <= split_cost) return leaf(first, count, lo, hi);
+            float ext = chi[best_axis] - clo[best_axis];
+            float k = (float)kBins / ext;
+            auto it = std::partition(idx.begin() + first, idx.begin() + first + count, [&](uint32_t i) {
+                int b = std::min(kBins - 1, (int)((prims[i].c[best_axis] - clo[best_axis]) * k));
+                return b <= best_bin;
+            });
+            mid = (uint32_t)(it - idx.begin());
+            if (mid == first || mid == first + count) mid = first + count / 2;
+        }
+        size_t node = nodes.size();
+        nodes.push_back(BvhNode{});
+        Ref l = build(first, mid - first, depth + 1);
+        Ref r = build(mid, first + count - mid, depth + 1);
+        BvhNode &n = nodes[node];
+        n.c0[0] = l.lo[0]; n.c0[1] = l.hi[0]; n.c0[2] = l.lo[1]; n.c0[3] = l.hi[1];
+        n.c1[0] = r.lo[0]; n.c1[1] = r.hi[0]; n.c1[2] = r.lo[1]; n.c1[3] = r.hi[1];
+        n.c2[0] = l.lo[2]; n.c2[1] = l.hi[2]; n.c2[2] = r.lo[2]; n.c2[3] = r.hi[2];
+        n.ref[0] = l.ref; n.ref[1] = r.ref;
+        n.count[0] = 0; n.count[1] = 0;
+        Ref me{(int32_t)node, 0, {lo[0], lo[1], lo[2]}, {hi[0], hi[1], hi[2]}};
+        return me;
+    }
+};
+
+// Boxes are padded so that culling stays conservative with respect to the triangle test's own
+// rounding: an absolute margin scaled by the coordinate magnitude.
+void pad_box(float lo[3], float hi[3]) {
+    for (int a = 0; a < 3; ++a) {
+        float m = std::max(std::fabs(lo[a]), std::fabs(hi[a]));
+        float pad = 1e-5f * std::max(1.0f, m);
+        lo[a] -= pad;
+        hi[a] += pad;
+    }
+}
+
+}  // namespace
+
+void build_bvh(HostScene &s) {
+    size_t n = s.occ_mesh.size();
+    s.nodes.clear();
+    s.tri_v0.assign(n * 4, 0.0f);
+    s.tri_e1.assign(n * 4, 0.0f);
+    s.tri_e2.assign(n * 4, 0.0f);
+    if (n == 0) return;
+    Builder b;
+    b.prims.resize(n);
+    std::vector<f3> v(n * 3);
+    for (size_t i = 0; i < n; ++i) {
+        const dl_mesh &m = *s.meshes[s.occ_mesh[i]];
+        Prim &p = b.prims[i];
+        for (int k = 0; k < 3; ++k) {
+            const float *q = m.positions + (size_t)m.indices[(size_t)s.occ_tri[i] * 3 + k] * 3;
+            v[i * 3 + k] = f3{q[0], q[1], q[2]};
+        }
+        for (int a = 0; a < 3; ++a) {
+            float x0 = axis_of(v[i * 3], a), x1 = axis_of(v[i * 3 + 1], a), x2 = axis_of(v[i * 3 + 2], a);
+            p.lo[a] = std::min(x0, std::min(x1, x2));
+            p.hi[a] = std::max(x0, std::max(x1, x2));
+            p.c[a] = (p.lo[a] + p.hi[a]) * 0.5f;
+        }
+    }
+    b.idx.resize(n);
+    std::iota(b.idx.begin(), b.idx.end(), 0u);
+    b.nodes.reserve(n);
+    b.nodes.push_back(BvhNode{});  // root placeholder
+    Ref root = b.build(0, (uint32_t)n, 1);
+    if (root.ref < 0) {
+        // the whole set is one leaf: the root holds it and an empty second child
+        BvhNode &r = b.nodes[0];
+        r.c0[0] = root.lo[0]; r.c0[1] = root.hi[0]; r.c0[2] = root.lo[1]; r.c0[3] = root.hi[1];
+        r.c2[0] = root.lo[2]; r.c2[1] = root.hi[2];
+        r.c1[0] = 1e30f; r.c1[1] = -1e30f; r.c1[2] = 1e30f; r.c1[3] = -1e30f;
+        r.c2[2] = 1e30f; r.c2[3] = -1e30f;
+        r.ref[0] = root.ref; r.ref[1] = ~0; r.count[0] = 0; r.count[1] = 0;
+    } else {
+        // move the built root (index root.ref) into slot 0
+        b.nodes[0] = b.nodes[(size_t)root.ref];
+        for (auto &nd : b.nodes)
+            for (int c = 0; c < 2; ++c)
+                if (nd.ref[c] == root.ref) nd.ref[c] = 0;
+    }
+    for (auto &nd : b.nodes) {
+        float lo[3] = {nd.c0[0], nd.c0[2], nd.c2[0]}, hi[3] = {nd.c0[1], nd.c0[3], nd.c2[1]};
+        if (nd.ref[0] != ~0) {
+            pad_box(lo, hi);
+            nd.c0[0] = lo[0]; nd.c0[1] = hi[0]; nd.c0[2] = lo[1]; nd.c0[3] = hi[1]; nd.c2[0] = lo[2]; nd.c2[1] = hi[2];
+        }
+        float lo1[3] = {nd.c1[0], nd.c1[2], nd.c2[2]}, hi1[3] = {nd.c1[1], nd.c1[3], nd.c2[3]};
+        if (nd.ref[1] != ~0) {
+            pad_box(lo1, hi1);
+            nd.c1[0] = lo1[0]; nd.c1[1] = hi1[0]; nd.c1[2] = lo1[1]; nd.c1[3] = hi1[1]; nd.c2[2] = lo1[2]; nd.c2[3] = hi1[2];
+        }
+    }
+    s.nodes = std::move(b.nodes);
+    s.bvh_depth = b.max_depth;
+    for (size_t k = 0; k < n; ++k) {
+        uint32_t i = b.idx[k];
+        f3 a = v[i * 3], e1 = sub(v[i * 3 + 1], a), e2 = sub(v[i * 3 + 2], a);
+        uint32_t bits = i;
+        float w;
+        std::memcpy(&w, &bits, 4);
+        float *p0 = &s.tri_v0[k * 4], *p1 = &s.tri_e1[k * 4], *p2 = &s.tri_e2[k * 4];
+        p0[0] = a.x; p0[1] = a.y; p0[2] = a.z; p0[3] = w;
+        p1[0] = e1.x; p1[1] = e1.y; p1[2] = e1.z; p1[3] = 0.0f;
+        p2[0] = e2.x; p2[1] = e2.y; p2[2] = e2.z; p2[3] = 0.0f;
+    }
+}
+
+// ---- payload (src/bake/format/mod.rs:170-213, lights.rs:27-52, maps.rs:16-37) -------------------
+namespace {
+struct Writer {
+    std::vector<uint8_t> b;
+    void u32(uint32_t v) { for (int i = 0; i < 4; ++i) b.push_back((uint8_t)(v >> (8 * i))); }
+    void u64(uint64_t v) { for (int i = 0; i < 8; ++i) b.push_back((uint8_t)(v >> (8 * i))); }
+    void f32(float f) { uint32_t v; std::memcpy(&v, &f, 4); u32(v); }
+    void words(const uint32_t *w, uint64_t n) { u64(n); for (uint64_t i = 0; i < n; ++i) u32(w[i]); }
+};
+}  // namespace
+
+std::vector<uint8_t> encode_payload(const dl_baked_scene &s) {
+    Writer w;
+    w.u32((s.settings.bounce ? 1u : 0u) | (s.settings.colored_bounce ? 2u : 0u));
+    w.u32(s.settings.dynamic_geometry);
+    w.f32(s.settings.pixel_density);
+    w.u32(s.settings.max_lightmap_size);
+    w.u32(s.settings.distance_cube_resolution);
+    w.u64(s.light_count);
+    for (uint64_t i = 0; i < s.light_count; ++i) {
+        const dl_baked_light &l = s.lights[i];
+        w.u64(l.id);
+        for (int k = 0; k < 3; ++k) w.f32(l.origin[k]);
+        w.f32(l.radius);
+        w.u32(l.bounce_bits);
+        w.u32(l.shape);
+        for (int k = 0; k < 4; ++k) w.f32(l.rotation[k]);
+        for (int k = 0; k < 2; ++k) w.f32(l.size[k]);
+        w.u32(l.shadow_bits_per_texel);
+    }
+    w.words(reinterpret_cast<const uint32_t *>(s.light_bvh), s.light_bvh_count * 8);
+    w.u64(s.mesh_count);
+    for (uint64_t i = 0; i < s.mesh_count; ++i) {
+        const dl_baked_mesh &m = s.meshes[i];
+        w.u64(m.id);
+        w.u64(m.content_hash);
+        w.u32(m.resolution);
+        w.u32(m.occludes ? 1u : 0u);
+        w.words(m.triangles, m.word_count);
+    }
+    w.words(s.distance_cubes, s.distance_cube_words);
+    w.u64(0);  // sun maps: none in LightingOnly
+    w.u32(0);  // no sky probes
+    w.u32(s.stats.meshes);
+    w.u64(s.stats.triangles);
+    w.u64(s.stats.texels);
+    w.u64(s.stats.rays);
+    w.u64(s.stats.lights_removed);
+    w.u64(s.stats.bounce_rays);
+    w.u64(s.stats.triangle_words);
+    return w.b;
+}
+
+// CRC-32 (IEEE 802.3, reflected polynomial 0xEDB88320), table-driven.
+uint32_t crc32_ieee(const uint8_t *data, size_t n) {
+    static uint32_t table[256];
+    static bool ready = false;
+    if (!ready) {
+        for (uint32_t i = 0; i < 256; ++i) {
+            uint32_t c = i;
+            for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+            table[i] = c;
+        }
+        ready = true;
+    }
+    uint32_t c = 0xFFFFFFFFu;
+    for (size_t i = 0; i < n; ++i) c = table[(c ^ data[i]) & 0xFF] ^ (c >> 8);
+    return c ^ 0xFFFFFFFFu;
+}
+
+}  // namespace dl

@@ -1,0 +1,334 @@
+// f32 arithmetic of the bake in the reference's operation order, for host and device.
+//
+// The library is compiled with --fmad=false (device) and -ffp-contract=off (host), so every
+// a*b+c below rounds twice exactly like the reference's Rust (src/bake/*.rs), which never
+// contracts. Vector conventions follow glam 0.33 as the reference uses it:
+//   dot(a, b) = (a.x*b.x + a.y*b.y) + a.z*b.z
+//   cross(a, b) = (a.y*b.z - b.y*a.z, a.z*b.x - b.z*a.x, a.x*b.y - b.x*a.y)
+//   normalize(v) = v * (1 / sqrt(dot(v, v)))
+// Transcendentals of f32 arguments are evaluated in binary64 (Cody–Waite reduction by pi/2 and
+// Taylor series) and rounded once, so host and device agree bit for bit and the result is the
+// correctly rounded f32 except for ~1e-8 of arguments.
+#pragma once
+
+#include <cstdint>
+#include <math.h>
+
+#if defined(__CUDACC__)
+#define DL_HD __host__ __device__ __forceinline__
+#else
+#define DL_HD inline
+#endif
+
+namespace dl {
+
+struct f2 {
+    float x, y;
+};
+struct f3 {
+    float x, y, z;
+};
+
+DL_HD f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
+DL_HD f3 add(f3 a, f3 b) { return f3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+DL_HD f3 sub(f3 a, f3 b) { return f3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+DL_HD f3 neg(f3 a) { return f3{-a.x, -a.y, -a.z}; }
+DL_HD f3 scale(f3 a, float s) { return f3{a.x * s, a.y * s, a.z * s}; }
+DL_HD f3 divs(f3 a, float s) { return f3{a.x / s, a.y / s, a.z / s}; }
+DL_HD float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+DL_HD f3 cross(f3 a, f3 b) { return f3{a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
+DL_HD bool is_zero(f3 a) { return a.x == 0.0f && a.y == 0.0f && a.z == 0.0f; }
+DL_HD float length_sq(f3 a) { return dot(a, a); }
+DL_HD float length(f3 a) { return sqrtf(dot(a, a)); }
+DL_HD bool finite_pos(float r) { return isfinite(r) && r > 0.0f; }
+DL_HD f3 normalize(f3 a) { return scale(a, 1.0f / length(a)); }
+DL_HD f3 normalize_or(f3 a, f3 fb) {
+    float r = 1.0f / length(a);
+    return finite_pos(r) ? scale(a, r) : fb;
+}
+DL_HD f3 normalize_or_zero(f3 a) { return normalize_or(a, f3{0.0f, 0.0f, 0.0f}); }
+DL_HD f3 try_normalize(f3 a, bool &ok) {
+    float r = 1.0f / length(a);
+    ok = finite_pos(r);
+    return ok ? scale(a, r) : f3{0.0f, 0.0f, 0.0f};
+}
+DL_HD float fminr(float a, float b) { return fminf(a, b); }
+DL_HD float fmaxr(float a, float b) { return fmaxf(a, b); }
+DL_HD f3 vmin(f3 a, f3 b) { return f3{fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z)}; }
+DL_HD f3 vmax(f3 a, f3 b) { return f3{fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z)}; }
+DL_HD float max_elem(f3 a) { return fmaxf(fmaxf(a.x, a.y), a.z); }
+DL_HD bool approx_eq(f3 a, f3 b, float eps) {
+    f3 d = sub(a, b);
+    return fmaxf(fmaxf(fabsf(d.x), fabsf(d.y)), fabsf(d.z)) < eps;
+}
+DL_HD float clampf(float v, float lo, float hi) {
+    if (v < lo) v = lo;
+    if (v > hi) v = hi;
+    return v;
+}
+// Rust `as u32` / `as u8` / `as i8`: saturating, NaN to 0.
+DL_HD uint32_t f2u(float f) {
+    if (!(f > 0.0f)) return 0u;
+    if (f >= 4294967296.0f) return 0xFFFFFFFFu;
+    return (uint32_t)f;
+}
+DL_HD uint32_t f2u8(float f) {
+    if (!(f > 0.0f)) return 0u;
+    if (f >= 255.0f) return 255u;
+    return (uint32_t)f;
+}
+DL_HD int f2i8(float f) {
+    if (isnan(f)) return 0;
+    if (f <= -128.0f) return -128;
+    if (f >= 127.0f) return 127;
+    return (int)f;
+}
+
+// Orthonormal basis around a unit vector (Duff et al., JCGT 2017), as glam's
+// Vec3::any_orthonormal_pair evaluates it.
+DL_HD void ortho_pair(f3 n, f3 &a, f3 &b) {
+    float sign = signbit(n.z) ? -1.0f : 1.0f;
+    float k = -1.0f / (sign + n.z);
+    float m = n.x * n.y * k;
+    a = f3{1.0f + sign * n.x * n.x * k, sign * m, -sign * n.x};
+    b = f3{m, sign + n.y * n.y * k, -n.y};
+}
+
+// Quaternion (x, y, z, w) times vector: v(w^2 - |q|^2) + q(2 v.q) + (q x v)(2w).
+DL_HD f3 quat_rotate(const float q[4], f3 v) {
+    f3 b{q[0], q[1], q[2]};
+    float w = q[3];
+    float b2 = dot(b, b);
+    return add(add(scale(v, w * w - b2), scale(b, dot(v, b) * 2.0f)), scale(cross(b, v), w * 2.0f));
+}
+
+// ---- transcendentals ---------------------------------------------------------------------------
+// pi/2 split for Cody–Waite reduction: the high part holds 33 significant bits.
+constexpr double kPio2Hi = 1.5707963267341256;     // 0x1.921fb54400000p+0
+constexpr double kPio2Lo = 6.077100506506192e-11;  // 0x1.0b4611a626331p-34
+constexpr double kTwoOverPi = 0.6366197723675814;
+constexpr double kPi = 3.141592653589793;
+
+// Taylor series of sin and cos on |r| <= pi/4 (coefficients (-1)^n/(2n+1)! and (-1)^n/(2n)!).
+DL_HD void sincos_poly(double r, double &s, double &c) {
+    double r2 = r * r;
+    double p = -3.868170170630684e-23;
+    p = p * r2 + 1.9572941063391263e-20;
+    p = p * r2 + -8.22063524662433e-18;
+    p = p * r2 + 2.8114572543455206e-15;
+    p = p * r2 + -7.647163731819816e-13;
+    p = p * r2 + 1.6059043836821613e-10;
+    p = p * r2 + -2.505210838544172e-08;
+    p = p * r2 + 2.7557319223985893e-06;
+    p = p * r2 + -0.0001984126984126984;
+    p = p * r2 + 0.008333333333333333;
+    p = p * r2 + -0.16666666666666666;
+    s = r + r * (r2 * p);
+    double q = -8.896791392450574e-22;
+    q = q * r2 + 4.110317623312165e-19;
+    q = q * r2 + -1.5619206968586225e-16;
+    q = q * r2 + 4.779477332387385e-14;
+    q = q * r2 + -1.1470745597729725e-11;
+    q = q * r2 + 2.08767569878681e-09;
+    q = q * r2 + -2.755731922398589e-07;
+    q = q * r2 + 2.48015873015873e-05;
+    q = q * r2 + -0.001388888888888889;
+    q = q * r2 + 0.041666666666666664;
+    q = q * r2 + -0.5;
+    c = 1.0 + r2 * q;
+}
+DL_HD void sincos_d(double x, double &s, double &c) {
+    double k = nearbyint(x * kTwoOverPi);
+    double r = (x - k * kPio2Hi) - k * kPio2Lo;
+    double sr, cr;
+    sincos_poly(r, sr, cr);
+    switch ((long long)k & 3) {
+        case 0: s = sr; c = cr; break;
+        case 1: s = cr; c = -sr; break;
+        case 2: s = -sr; c = -cr; break;
+        default: s = -cr; c = sr; break;
+    }
+}
+DL_HD void sincos_f(float x, float &s, float &c) {
+    if (!isfinite(x)) {
+        s = c = NAN;
+        return;
+    }
+    double sd, cd;
+    sincos_d((double)x, sd, cd);
+    s = (float)sd;
+    c = (float)cd;
+}
+DL_HD float sin_f(float x) {
+    float s, c;
+    sincos_f(x, s, c);
+    return s;
+}
+DL_HD float tan_f(float x) {
+    if (!isfinite(x)) return NAN;
+    double s, c;
+    sincos_d((double)x, s, c);
+    return (float)(s / c);
+}
+// asin on |y| <= 1/2 by its Maclaurin series, coefficients (2n)!/(4^n (n!)^2 (2n+1)).
+DL_HD double asin_series(double y) {
+    double y2 = y * y;
+    double p = 0.0022014739737101384;
+    p = p * y2 + 0.002338091892111975;
+    p = p * y2 + 0.0024894486782468836;
+    p = p * y2 + 0.00265787063820729;
+    p = p * y2 + 0.002846178401108942;
+    p = p * y2 + 0.0030578216492580306;
+    p = p * y2 + 0.003297059503473485;
+    p = p * y2 + 0.0035692053938259347;
+    p = p * y2 + 0.003880964558837669;
+    p = p * y2 + 0.004240907093679363;
+    p = p * y2 + 0.004660143486915096;
+    p = p * y2 + 0.005153309682319905;
+    p = p * y2 + 0.005740037670841924;
+    p = p * y2 + 0.006447210311889649;
+    p = p * y2 + 0.0073125258735988454;
+    p = p * y2 + 0.008390335809616815;
+    p = p * y2 + 0.009761609529194078;
+    p = p * y2 + 0.011551800896139705;
+    p = p * y2 + 0.01396484375;
+    p = p * y2 + 0.017352764423076924;
+    p = p * y2 + 0.022372159090909092;
+    p = p * y2 + 0.030381944444444444;
+    p = p * y2 + 0.044642857142857144;
+    p = p * y2 + 0.075;
+    p = p * y2 + 0.16666666666666666;
+    p = p * y2 + 1.0;
+    return y * p;
+}
+DL_HD float acos_f(float xf) {
+    double x = (double)xf;
+    if (isnan(x) || x > 1.0 || x < -1.0) return NAN;
+    double r;
+    if (fabs(x) <= 0.5)
+        r = (kPio2Hi + kPio2Lo) - asin_series(x);
+    else if (x > 0.0)
+        r = 2.0 * asin_series(sqrt((1.0 - x) * 0.5));
+    else
+        r = kPi - 2.0 * asin_series(sqrt((1.0 + x) * 0.5));
+    return (float)r;
+}
+
+constexpr float kTau = 6.28318530717958647692f;
+constexpr float kPiF = 3.14159265358979323846f;
+constexpr float kFracPi4 = 0.78539816339744830962f;
+constexpr float kNdotlTolerance = -0.1f;  // mesh_bake.rs:25
+constexpr float kRayOffset = 0.001f;      // mesh_bake.rs:27
+constexpr float kEndGap = 1.0e-3f;        // area.rs:33
+
+// ---- RNG: SplitMix64 + PCG32 XSH-RR keyed streams (src/effects/rng.rs:10-71,
+// src/bake/random.rs:9-19) --------------------------------------------------------------------
+DL_HD uint64_t splitmix64(uint64_t v) {
+    v += 0x9e3779b97f4a7c15ull;
+    v = (v ^ (v >> 30)) * 0xbf58476d1ce4e5b9ull;
+    v = (v ^ (v >> 27)) * 0x94d049bb133111ebull;
+    return v ^ (v >> 31);
+}
+DL_HD uint64_t fold_seed(uint64_t acc, uint64_t part) { return splitmix64(acc ^ splitmix64(part)); }
+constexpr uint64_t kSeedStart = 0x0b4ce5eed0000000ull;
+
+struct Pcg {
+    uint64_t state, inc;
+    DL_HD uint32_t next_u32() {
+        uint64_t old = state;
+        state = old * 6364136223846793005ull + inc;
+        uint32_t xs = (uint32_t)(((old >> 18) ^ old) >> 27);
+        uint32_t rot = (uint32_t)(old >> 59);
+        return (xs >> rot) | (xs << ((32u - rot) & 31u));
+    }
+    DL_HD float next_f32() { return (float)(next_u32() >> 8) * (1.0f / 16777216.0f); }
+};
+DL_HD Pcg pcg_new(uint64_t seed, uint64_t stream) {
+    Pcg r{0, (stream << 1) | 1};
+    r.next_u32();
+    r.state += seed;
+    r.next_u32();
+    return r;
+}
+DL_HD Pcg pcg_from_seed(uint64_t s) { return pcg_new(s, (s << 17) | (s >> 47)); }
+// stream([a, b, c, ...]) for the key lengths the bake uses.
+DL_HD Pcg stream4(uint64_t a, uint64_t b, uint64_t c, uint64_t d) {
+    return pcg_from_seed(fold_seed(fold_seed(fold_seed(fold_seed(kSeedStart, a), b), c), d));
+}
+DL_HD Pcg stream5(uint64_t a, uint64_t b, uint64_t c, uint64_t d, uint64_t e) {
+    return pcg_from_seed(fold_seed(fold_seed(fold_seed(fold_seed(fold_seed(kSeedStart, a), b), c), d), e));
+}
+DL_HD Pcg stream6(uint64_t a, uint64_t b, uint64_t c, uint64_t d, uint64_t e, uint64_t f) {
+    return pcg_from_seed(
+        fold_seed(fold_seed(fold_seed(fold_seed(fold_seed(fold_seed(kSeedStart, a), b), c), d), e), f));
+}
+// random.rs:22-27
+DL_HD f3 on_unit_sphere(Pcg &rng) {
+    float z = rng.next_f32() * 2.0f - 1.0f;
+    float angle = rng.next_f32() * kTau;
+    float r = sqrtf(fmaxf(1.0f - z * z, 0.0f));
+    float s, c;
+    sincos_f(angle, s, c);
+    return f3{r * c, r * s, z};
+}
+
+// ---- low-discrepancy points (src/bake/spread.rs) ----------------------------------------------
+DL_HD uint32_t rev_bits(uint32_t v) {
+#if defined(__CUDA_ARCH__)
+    return __brev(v);
+#else
+    v = ((v >> 1) & 0x55555555u) | ((v & 0x55555555u) << 1);
+    v = ((v >> 2) & 0x33333333u) | ((v & 0x33333333u) << 2);
+    v = ((v >> 4) & 0x0F0F0F0Fu) | ((v & 0x0F0F0F0Fu) << 4);
+    v = ((v >> 8) & 0x00FF00FFu) | ((v & 0x00FF00FFu) << 8);
+    return (v >> 16) | (v << 16);
+#endif
+}
+DL_HD uint32_t sobol2(uint32_t index) {
+    uint32_t value = 0, dir = 1u << 31;
+    while (index != 0) {
+        if (index & 1u) value ^= dir;
+        index >>= 1;
+        dir ^= dir >> 1;
+    }
+    return value;
+}
+DL_HD float unit24(uint32_t bits) { return (float)(bits >> 8) / 16777216.0f; }
+DL_HD f2 spread(uint32_t index, f2 off, bool rect) {
+    float across = unit24(rev_bits(index));
+    float down = rect ? unit24(sobol2(index)) : 0.0f;
+    float a = across + off.x, d = down + off.y;
+    return f2{a - floorf(a), d - floorf(d)};
+}
+// Shirley–Chiu concentric map (spread.rs:28-39).
+DL_HD f2 concentric(f2 sq) {
+    float px = sq.x * 2.0f - 1.0f, py = sq.y * 2.0f - 1.0f;
+    if (px == 0.0f && py == 0.0f) return f2{0.0f, 0.0f};
+    float radius, angle;
+    if (fabsf(px) > fabsf(py)) {
+        radius = px;
+        angle = kFracPi4 * (py / px);
+    } else {
+        radius = py;
+        angle = 2.0f * kFracPi4 - kFracPi4 * (px / py);
+    }
+    float s, c;
+    sincos_f(angle, s, c);
+    return f2{c * radius, s * radius};
+}
+// Malley's method (sky.rs:20-25).
+DL_HD f3 cosine_direction(f3 n, f2 sq) {
+    f2 d = concentric(sq);
+    float up = sqrtf(fmaxf(1.0f - (d.x * d.x + d.y * d.y), 0.0f));
+    f3 side, across;
+    ortho_pair(n, side, across);
+    return normalize(add(add(scale(side, d.x), scale(across, d.y)), scale(n, up)));
+}
+
+// shadow_grid.rs:13-16
+DL_HD uint32_t level_of(float fraction, uint32_t bits) {
+    float max = (float)((1u << bits) - 1);
+    return f2u8(roundf(clampf(fraction, 0.0f, 1.0f) * max));
+}
+
+}  // namespace dl

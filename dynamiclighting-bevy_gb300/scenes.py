@@ -264,8 +264,8 @@ def room_grid(seed=2, rooms=6, lights=64, boxes_per_room=20, bounce=True, cell=0
         for ix in range(rooms):
             ox, oz = ix * (ROOM + GAP), iz * (ROOM + GAP)
             c = cell
-            if soft:  # log-normal surface subdivision: per room a cell size around 0.56 m
-                c = float(np.clip(0.56 * math.exp(rng.uniform(-1.6, 1.6)), 0.09, 5.6))
+            if soft:  # log-normal surface subdivision: per room a cell size around 0.8 m
+                c = float(np.clip(0.8 * math.exp(rng.uniform(-1.0, 1.6)), 0.28, 5.6))
             a = rng.uniform(0.2, 0.8)
             meshes.append(_room_shell(mesh_id, ox, oz, rooms, rooms, ix, iz, c, (a, a, a)))
             mesh_id += 1

@@ -1,0 +1,170 @@
+"""GPU parity: the CUDA bake (both forms) against the oracle, word for word.
+
+Every comparison is of the final per-mesh `dynamic_triangles` words (the per-pair shadow bit and
+level layout, src/bake/triangle_words.rs:1-13) plus the bake statistics; integer outputs, so the
+bar is bit-exact."""
+import math
+
+import numpy as np
+import pytest
+
+import dynlight_gb300 as dl
+from dynlight_gb300 import scenes
+from oracle import oracle
+
+from . import fixtures as fx
+
+pytestmark = pytest.mark.gpu
+
+
+def first_difference(a, b):
+    for ma, mb in zip(a.meshes, b.meshes):
+        if ma.id != mb.id or ma.resolution != mb.resolution:
+            return f"mesh {ma.id}/{mb.id}: resolution {ma.resolution}/{mb.resolution}"
+        if len(ma.triangles) != len(mb.triangles):
+            return f"mesh {ma.id}: {len(ma.triangles)} vs {len(mb.triangles)} words"
+        d = np.nonzero(ma.triangles != mb.triangles)[0]
+        if len(d):
+            return f"mesh {ma.id}: {len(d)} words differ, first at {d[0]}"
+    return None
+
+
+def assert_same(got, want):
+    assert len(got.meshes) == len(want.meshes)
+    assert got.words_equal(want), first_difference(got, want)
+    assert got.stats == want.stats
+    assert [l.id for l in got.lights] == [l.id for l in want.lights]
+    assert np.array_equal(got.light_bvh, want.light_bvh)
+    assert got.settings == want.settings
+
+
+@pytest.mark.parametrize("form", ["batched", "plain"])
+def test_small_room_matches_the_oracle(form):
+    inp, opts = scenes.small_room()
+    want, _, _ = oracle.bake(inp, opts)
+    report = dl._abi.DlBakeReport()
+    got = dl.bake(inp, opts, form=form, report=report)
+    assert_same(got, want)
+    assert report.kernel_launches > 0 and report.shadow_rays == want.stats["rays"]
+
+
+@pytest.mark.parametrize("form", ["batched", "plain"])
+def test_mixed_lights_match_the_oracle(form):
+    # points, a panel, a tube, a soft and a hard sun, a sky (src/bake/tests/determinism.rs:11-44)
+    inp, opts = fx.determinism_room()
+    want, _, _ = oracle.bake(inp, opts)
+    got = dl.bake(inp, opts, form=form)
+    assert_same(got, want)
+    bits = sorted({l.shadow_bits_per_texel for l in got.lights})
+    assert bits == [1, 4, 8]
+
+
+def test_soft_rooms_batched_and_plain_agree_with_the_oracle():
+    inp, opts = scenes.soft_rooms(rooms=2, lights=24, boxes_per_room=6)
+    want, _, _ = oracle.bake(inp, opts)
+    batched = dl.bake(inp, opts, form="batched")
+    plain = dl.bake(inp, opts, form="plain")
+    assert_same(batched, want)
+    assert_same(plain, want)
+
+
+def test_outdoor_slice_with_sun_and_sky():
+    inp, opts = scenes.outdoor(grid=65, chunks=2, boxes=40, point_lights=6, sky_samples=32,
+                               bounce_samples=8)
+    for l in inp.lights:
+        l.illumination = dl.DIRECT
+    want, _, _ = oracle.bake(inp, opts)
+    got = dl.bake(inp, opts)
+    assert_same(got, want)
+
+
+def test_alpha_tested_shadows():
+    # a half-transparent plane (src/bake/tests/occluder.rs:85-98) over a floor
+    plane = fx.floor(1, (0, 1.0, 0), 1.0)
+    plane.uv0 = plane.uv1.copy()
+    plane.alpha = dl.AlphaTexture(2, 1, np.array([255, 255, 255, 0, 255, 255, 255, 255], np.uint8))
+    ground = fx.floor(2, (0, 0, 0), 2.0)
+    lights = [fx.point_light(5, (0.1, 3.0, 0.2), 6.0, transparency=dl.TRANSPARENCY_ENABLED),
+              fx.point_light(6, (0.3, 2.5, -0.2), 6.0)]
+    inp = dl.BakeInput([plane, ground], lights)
+    opts = fx.options(pixel_density=16.0)
+    want, _, _ = oracle.bake(inp, opts)
+    assert_same(dl.bake(inp, opts), want)
+
+
+def test_thin_and_buried_geometry():
+    # a pipe strip narrower than a texel and a box sunk into the floor
+    # (src/bake/tests/coverage.rs:63-160 cover both cases)
+    strip = dl.BakeMesh(id=3, positions=np.float32([[0, 0.5, 0], [2, 0.5, 0], [2, 0.5, 0.02], [0, 0.5, 0.02]]),
+                        indices=np.uint32([0, 2, 1, 0, 3, 2]),
+                        uv1=np.float32([[0.1, 0.1], [0.9, 0.1], [0.9, 0.103], [0.1, 0.103]]))
+    sunk = fx.cuboid(4, (-1.0, -0.5, -1.0), (-0.2, 0.3, -0.2))
+    ground = fx.floor(2, (0, 0, 0), 2.0)
+    inp = dl.BakeInput([strip, sunk, ground], [fx.point_light(9, (0.5, 2.0, 0.5), 5.0)])
+    opts = fx.options(pixel_density=24.0)
+    want, burial, _ = oracle.bake(inp, opts)
+    assert burial > 0
+    assert_same(dl.bake(inp, opts), want)
+
+
+def test_empty_and_lightless_scenes():
+    empty, opts = dl.BakeInput(), fx.options(pixel_density=12.0)
+    got = dl.bake(empty, opts)
+    assert got.meshes == [] and got.lights == [] and len(got.light_bvh) == 0
+    lone = dl.BakeInput([fx.floor(1, (0, 0, 0), 1.0)], [])
+    got = dl.bake(lone, opts)
+    want, _, _ = oracle.bake(lone, opts)
+    assert_same(got, want)
+    assert got.meshes[0].triangle_count() == 2
+
+
+def test_errors_mirror_the_reference():
+    inp, opts = fx.determinism_room()
+    inp.meshes[1].id = 5
+    with pytest.raises(dl.BakeError) as e:
+        dl.bake(inp, opts)
+    assert e.value.kind == "DuplicateId"
+    inp, opts = fx.determinism_room()
+    inp.lights[0].radius = 0.0
+    with pytest.raises(dl.BakeError) as e:
+        dl.bake(inp, opts)
+    assert e.value.kind == "InvalidLight"
+    inp, opts = fx.determinism_room()
+    inp.meshes[0].indices = np.append(inp.meshes[0].indices, np.uint32(99))
+    with pytest.raises(dl.BakeError) as e:
+        dl.bake(inp, opts)
+    assert e.value.kind == "InvalidMesh"
+    inp, opts = fx.determinism_room()
+    opts.pixel_density = -1.0
+    with pytest.raises(dl.BakeError) as e:
+        dl.bake(inp, opts)
+    assert e.value.kind == "InvalidOptions"
+
+
+def test_cancelled_bakes_stop():
+    inp, opts = fx.determinism_room()
+    progress = dl.BakeProgress()
+    progress.cancel()
+    with pytest.raises(dl.BakeError) as e:
+        dl.bake(inp, opts, progress=progress)
+    assert e.value.kind == "Cancelled"
+
+
+def test_sessions_repeat_identically():
+    inp, opts = scenes.small_room()
+    s = dl.Session(inp, opts)
+    s.run()
+    a = s.result()
+    s.run()
+    b = s.result()
+    s.close()
+    assert a.words_equal(b) and a.stats == b.stats
+
+
+def test_tuning_does_not_change_the_bytes():
+    # the GPU analogue of the reference's 1/4/7-thread determinism (determinism.rs:65-72)
+    inp, opts = scenes.soft_rooms(rooms=2, lights=16, boxes_per_room=4)
+    base = dl.bake(inp, opts)
+    for tuning in [dict(chunk_texels=128), dict(blocks_per_sm=1), dict(chunk_texels=32, blocks_per_sm=2)]:
+        other = dl.bake(inp, opts, **tuning)
+        assert other.words_equal(base) and other.stats == base.stats, tuning
