@@ -208,10 +208,22 @@ def main():
         t_max = float(t.item())
     value = rays * world / (t_max / 1e3)
 
-    # roofline of the dominant kernel (the persistent visibility kernel)
-    counted = dl.Session(inp, opts, form="batched", device=local, count_visits=1) if False else None
+    # roofline of the dominant kernel (the persistent visibility kernel): algorithmic bytes from
+    # an instrumented run of the same kernel on the same BVH (node visits x 64 B, triangle tests
+    # x 48 B) plus the per-item texel/pair reads and result writes (76 B per (pair, texel) item)
+    counted = dl.Session(inp, opts, form="batched", device=local, count_visits=1)
+    counted.run()
+    crep = counted.report()
+    counted.close()
     vis = statistics.median(vis_ms)
     hbm, peak_kind = peaks()
+    alg_bytes = crep.node_visits * 64 + crep.tri_tests * 48 + crep.work_items * 76
+    achieved = alg_bytes / (vis / 1e3) / 1e9 if vis > 0 else 0.0
+    traffic = None
+    traffic_path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(traffic_path):
+        with open(traffic_path) as f:
+            traffic = json.load(f).get(args.workload)
 
     # end to end through dl_bake from host buffers
     e2e_ms = []
@@ -244,7 +256,11 @@ def main():
         "gpu_launches": int(rep.kernel_launches),
         "e2e": {"value": e2e_value, "unit": "rays/s", "ms": statistics.median(e2e_ms),
                 "h2d_bytes_per_step": int(e2e_rep.h2d_bytes), "d2h_bytes_per_step": int(e2e_rep.d2h_bytes)},
-        "roofline": None,
+        "roofline": {"bound": "hbm", "kernel": "k_trace_batched", "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "traffic": traffic, "algorithmic_bytes_per_launch": int(alg_bytes),
+                     "node_visits": int(crep.node_visits), "tri_tests": int(crep.tri_tests),
+                     "items": int(crep.work_items)},
     }
     if not args.no_cpu_baseline:
         cb = cpu_baseline(args.workload)

@@ -372,6 +372,8 @@ def make_config(form="batched", **tuning) -> DlBakeConfig:
     cfg = DlBakeConfig()
     cfg.form = FORMS[form] if isinstance(form, str) else int(form)
     for k, v in tuning.items():
+        if not hasattr(cfg, k):
+            raise TypeError(f"unknown bake tuning {k!r}")
         setattr(cfg, k, int(v))
     return cfg
 

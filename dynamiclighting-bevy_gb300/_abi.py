@@ -54,7 +54,8 @@ class DlProgress(C.Structure):
 class DlBakeConfig(C.Structure):
     _fields_ = [("form", C.c_uint32), ("device", C.c_uint32), ("block_threads", C.c_uint32),
                 ("chunk_texels", C.c_uint32), ("sample_lanes", C.c_uint32),
-                ("blocks_per_sm", C.c_uint32), ("reserved", C.c_uint32 * 8)]
+                ("blocks_per_sm", C.c_uint32), ("count_visits", C.c_uint32),
+                ("reserved", C.c_uint32 * 7)]
 
 
 class DlBakeReport(C.Structure):
@@ -64,7 +65,8 @@ class DlBakeReport(C.Structure):
                 ("burial_rays", C.c_uint64), ("photon_rays", C.c_uint64), ("pairs", C.c_uint64),
                 ("work_items", C.c_uint64), ("kernel_launches", C.c_uint64),
                 ("bvh_nodes", C.c_uint64), ("occluders", C.c_uint64), ("h2d_bytes", C.c_uint64),
-                ("d2h_bytes", C.c_uint64), ("device_bytes", C.c_uint64)]
+                ("d2h_bytes", C.c_uint64), ("device_bytes", C.c_uint64),
+                ("node_visits", C.c_uint64), ("tri_tests", C.c_uint64)]
 
 
 class DlLightBvhNode(C.Structure):

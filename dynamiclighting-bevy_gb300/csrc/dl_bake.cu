@@ -38,6 +38,7 @@ constexpr uint64_t kBurialStream = 0x627572696564ull;  // mesh_texels.rs:26
 
 struct Counters {
     unsigned long long rays, burial_rays, lights_removed, bounce_rays, photon_rays, cancelled;
+    unsigned long long node_visits, tri_tests;  // instrumented visibility kernel only
 };
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
@@ -287,8 +288,9 @@ struct TraceArgs {
 };
 
 // One (pair, texel) of the visibility loop (mesh_bake.rs:231-248); returns the rays traced.
+template <bool COUNT = false>
 __device__ __forceinline__ uint32_t trace_texel(const DevScene &sc, const TraceArgs &a, uint32_t p, uint32_t k,
-                                                int *stack, int stride) {
+                                                int *stack, int stride, Visits *vis = nullptr) {
     uint32_t t = a.pair_tri[p], s = a.pair_light[p];
     uint32_t m = sc.tri_mesh[t];
     uint32_t ci = a.ctex_off[t] + k;
@@ -298,7 +300,7 @@ __device__ __forceinline__ uint32_t trace_texel(const DevScene &sc, const TraceA
     f3 pos{pp.x, pp.y, pp.z}, nrm{nn.x, nn.y, nn.z};
     f3 origin = add(pos, scale(f3{f.x, f.y, f.z}, kRayOffset));
     const DevLight &l = sc.lights[s];
-    Tracer tr{sc, origin, (l.flags & kLightAlpha) != 0, stack, stride};
+    Tracer<COUNT> tr{sc, origin, (l.flags & kLightAlpha) != 0, stack, stride, vis};
     Vis v = texel_shadow(sc, s, sc.mesh_id[m], x, y, pos, nrm, tr);
     if (!v.some) return 0;
     uint32_t res = sc.mesh_res[m];
@@ -328,11 +330,13 @@ __device__ __forceinline__ uint32_t trace_texel(const DevScene &sc, const TraceA
 
 // Batched form: persistent warps pull chunks of (pair, texel) items from one queue. Items are
 // ordered sky pairs first, then soft, then hard, so the longest work starts first.
+template <bool COUNT>
 __global__ void __launch_bounds__(kBlock) k_trace_batched(DevScene sc, TraceArgs a) {
     __shared__ int stack[kStack * kBlock];
     int *my = stack + threadIdx.x;
     unsigned lane = lane_id();
     unsigned long long rays = 0;
+    Visits vis{0, 0};
     uint32_t grabs = 0;
     for (;;) {
         unsigned long long base = 0;
@@ -354,12 +358,20 @@ __global__ void __launch_bounds__(kBlock) k_trace_batched(DevScene sc, TraceArgs
             unsigned long long item = base + (unsigned long long)g * 32 + lane;
             if (item < a.items) {
                 while ((unsigned long long)a.item_off[cur + 1] <= item) ++cur;
-                rays += trace_texel(sc, a, a.order[cur], (uint32_t)(item - a.item_off[cur]), my, kBlock);
+                rays += trace_texel<COUNT>(sc, a, a.order[cur], (uint32_t)(item - a.item_off[cur]), my, kBlock,
+                                           &vis);
             }
         }
     }
     unsigned long long r = warp_sum(rays);
     if (lane == 0 && r) atomicAdd(&a.ctr->rays, r);
+    if (COUNT) {
+        unsigned long long n = warp_sum(vis.nodes), t = warp_sum(vis.tris);
+        if (lane == 0) {
+            atomicAdd(&a.ctr->node_visits, n);
+            atomicAdd(&a.ctr->tri_tests, t);
+        }
+    }
 }
 
 // Plain form: one launch per mesh; a warp per triangle, its lights in order, lanes over texels.
@@ -656,6 +668,13 @@ struct CudaError {
         if (e__ != cudaSuccess) throw CudaError{e__, #x};          \
     } while (0)
 
+// Launch errors surface here, named by the kernel that caused them.
+#define LAUNCHED(name)                                       \
+    do {                                                     \
+        cudaError_t e__ = cudaGetLastError();                \
+        if (e__ != cudaSuccess) throw CudaError{e__, name};  \
+    } while (0)
+
 template <class T>
 T *dev_alloc(std::vector<void *> &owned, size_t count, uint64_t &bytes) {
     void *p = nullptr;
@@ -764,7 +783,7 @@ T read_back(dl_session &s, const T *p) {
     CK(cudaStreamSynchronize(s.stream));
     return v;
 }
-unsigned grid_for(size_t n, unsigned block = kBlock) { return (unsigned)((n + block - 1) / block); }
+unsigned grid_for(size_t n, unsigned block = kBlock) { return (unsigned)std::max<size_t>(1, (n + block - 1) / block); }
 
 // Blocks the caller until the stream drains, forwarding a cancel request to the device flag.
 void wait(dl_session &s, dl_progress *progress) {
@@ -948,6 +967,23 @@ dl_status run(dl_session &s, dl_progress *progress) {
     CK(cudaEventRecord(e0, st));
     CK(cudaMemsetAsync(s.ctr, 0, sizeof(Counters), st));
     CK(cudaMemsetAsync(s.cancel_dev, 0, 4, st));
+    if (T == 0) {
+        // no triangles: every mesh serializes to no words (triangle_words.rs:47-56)
+        CK(cudaEventRecord(v0, st));
+        CK(cudaEventRecord(v1, st));
+        CK(cudaEventRecord(e1, st));
+        CK(cudaStreamSynchronize(st));
+        s.mesh_words.assign(M + 1, 0);
+        s.counters = Counters{};
+        s.out_words = 0;
+        s.words_dev = nullptr;
+        s.texels = 0;
+        s.report.ms_device = s.report.ms_visibility = 0.0;
+        s.report.pairs = 0;
+        s.report.kernel_launches = 0;
+        s.have_result = true;
+        return DL_OK;
+    }
 
     // ---- setup + association
     float4 *tri_face = P.get<float4>("tri_face", T);
@@ -957,6 +993,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
     CK(cudaMemsetAsync(tri_cnt + T, 0, 4, st));
     if (T) {
         k_setup<<<grid_for(T), kBlock, 0, st>>>(sc, tri_face, tri_crop, tri_cnt);
+        LAUNCHED("k_setup");
         ++s.launches;
     }
     scan_u32(s, tri_cnt, tri_off, T + 1);
@@ -967,17 +1004,20 @@ dl_status run(dl_session &s, dl_progress *progress) {
     uint32_t *region_rect = P.get<uint32_t>("region_rect", entries * 4);
     if (entries) {
         k_fill_u32<<<grid_for(entries * 4), kBlock, 0, st>>>(region_rect, entries * 4, kNoRect, 0u);
+        LAUNCHED("k_fill_u32");
         ++s.launches;
     }
     if (T) {
         k_assoc_fill<<<grid_for(T), kBlock, 0, st>>>(sc, tri_face, tri_crop, tri_off, pair_light, pair_tri,
                                                      region_rect);
+        LAUNCHED("k_assoc_fill");
         ++s.launches;
     }
     uint32_t *region_words = P.get<uint32_t>("region_words", entries + 1);
     uint32_t *region_off = P.get<uint32_t>("region_off", entries + 1);
     k_region_words<<<grid_for(entries + 1), kBlock, 0, st>>>(region_rect, sc.lights, (uint32_t)entries, L ? L : 1,
                                                              region_words);
+    LAUNCHED("k_region_words");
     ++s.launches;
     scan_u32(s, region_words, region_off, entries + 1);
     const uint32_t region_total = read_back(s, region_off + entries);
@@ -999,11 +1039,14 @@ dl_status run(dl_session &s, dl_progress *progress) {
     if (T) {
         k_texels<0><<<warp_grid, kBlock, 0, st>>>(sc, tri_face, owned, grid_off, cen, nullptr, nullptr, nullptr,
                                                   nullptr, nullptr);
+        LAUNCHED("k_texels");
         k_texels<1><<<warp_grid, kBlock, 0, st>>>(sc, tri_face, owned, grid_off, tou, nullptr, nullptr, nullptr,
                                                   nullptr, nullptr);
+        LAUNCHED("k_texels");
         s.launches += 2;
     }
     k_add_u32<<<grid_for(T + 1), kBlock, 0, st>>>(cen, tou, tex_cnt, T);
+    LAUNCHED("k_add_u32");
     ++s.launches;
     scan_u32(s, tex_cnt, tex_off, T + 1);
     const uint32_t texels_all = read_back(s, tex_off + T);
@@ -1015,11 +1058,13 @@ dl_status run(dl_session &s, dl_progress *progress) {
     if (T) {
         k_texels<2><<<warp_grid, kBlock, 0, st>>>(sc, tri_face, owned, grid_off, nullptr, tex_off, tex_xy, tex_pos,
                                                   tex_nrm, tex_tri);
+        LAUNCHED("k_texels");
         ++s.launches;
     }
     if (texels_all) {
         k_burial<<<grid_for(texels_all), kBlock, 0, st>>>(sc, texels_all, tex_xy, tex_pos, tex_tri, tri_face, buried,
                                                           s.ctr);
+        LAUNCHED("k_burial");
         ++s.launches;
     }
     uint32_t *ctex_cnt = P.get<uint32_t>("ctex_cnt", T + 1);
@@ -1028,6 +1073,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
     if (T) {
         k_unburied<false><<<warp_grid, kBlock, 0, st>>>(T, tex_off, buried, ctex_cnt, nullptr, nullptr, nullptr,
                                                         nullptr, nullptr, nullptr, nullptr);
+        LAUNCHED("k_unburied");
         ++s.launches;
     }
     scan_u32(s, ctex_cnt, ctex_off, T + 1);
@@ -1038,6 +1084,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
     if (T) {
         k_unburied<true><<<warp_grid, kBlock, 0, st>>>(T, tex_off, buried, nullptr, ctex_off, tex_xy, tex_pos,
                                                        tex_nrm, ctex_xy, ctex_pos, ctex_nrm);
+        LAUNCHED("k_unburied");
         ++s.launches;
     }
     s.texels = texels;
@@ -1066,6 +1113,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
             if (!count) continue;
             unsigned blocks = (unsigned)std::min<size_t>(grid_for((size_t)count * 32), (size_t)s.sms * 16);
             k_trace_plain<<<blocks, kBlock, 0, st>>>(sc, ta, first, count, tri_off);
+            LAUNCHED("k_trace_plain");
             ++s.launches;
             if (progress) progress->done = m + 1;
         }
@@ -1078,14 +1126,17 @@ dl_status run(dl_session &s, dl_progress *progress) {
         uint32_t base = 0;
         for (uint32_t c = 0; c < 3; ++c) {
             k_pair_class<<<grid_for(pairs + 1), kBlock, 0, st>>>(sc, pair_light, pairs, c, flag);
+            LAUNCHED("k_pair_class");
             scan_u32(s, flag, fpos, pairs + 1);
             k_pair_scatter<<<grid_for(pairs), kBlock, 0, st>>>(flag, fpos, pairs, base, order);
+            LAUNCHED("k_pair_scatter");
             s.launches += 2;
             base += read_back(s, fpos + pairs);
         }
         uint32_t *icnt = P.get<uint32_t>("icnt", pairs + 1);
         uint32_t *item_off = P.get<uint32_t>("item_off", pairs + 1);
         k_item_counts<<<grid_for(pairs + 1), kBlock, 0, st>>>(order, pair_tri, ctex_off, pairs, icnt);
+        LAUNCHED("k_item_counts");
         ++s.launches;
         scan_u32(s, icnt, item_off, pairs + 1);
         const uint32_t items = read_back(s, item_off + pairs);
@@ -1098,7 +1149,9 @@ dl_status run(dl_session &s, dl_progress *progress) {
         ta.head = head;
         ta.grab = s.config.chunk_texels ? std::max(1u, s.config.chunk_texels / 32) : 1;
         int per_sm = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_batched, kBlock, 0));
+        const bool count = s.config.count_visits != 0;  // instrumented variant: counts node visits
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, count ? k_trace_batched<true> : k_trace_batched<false>,
+                                                         kBlock, 0));
         if (s.config.blocks_per_sm) per_sm = std::min(per_sm, (int)s.config.blocks_per_sm);
         unsigned blocks = (unsigned)std::max(1, per_sm * s.sms);
         // The visibility stage runs from a CUDA graph: the memset of the queue head and the
@@ -1109,7 +1162,8 @@ dl_status run(dl_session &s, dl_progress *progress) {
             cudaGraph_t g;
             CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
             cudaMemsetAsync(head, 0, sizeof(unsigned long long), st);
-            if (items) k_trace_batched<<<blocks, kBlock, 0, st>>>(sc, ta);
+            if (items && count) k_trace_batched<true><<<blocks, kBlock, 0, st>>>(sc, ta);
+            if (items && !count) k_trace_batched<false><<<blocks, kBlock, 0, st>>>(sc, ta);
             CK(cudaStreamEndCapture(st, &g));
             CK(cudaGraphInstantiate(&s.graph, g, 0));
             cudaGraphDestroy(g);
@@ -1135,11 +1189,13 @@ dl_status run(dl_session &s, dl_progress *progress) {
     if (T) {
         k_optimize<<<grid_for(T), kBlock, 0, st>>>(sc, tri_off, pair_light, region_rect, region_off, region_pool,
                                                    nullptr, keep, kept_cnt, used, s.ctr);
+        LAUNCHED("k_optimize");
         ++s.launches;
     }
     if (entries) {
         k_pad_seams<<<(unsigned)entries, kBlock, 0, st>>>(sc, used, region_rect, region_off, region_pool, visited,
                                                           grid_off);
+        LAUNCHED("k_pad_seams");
         ++s.launches;
     }
     scan_u32(s, kept_cnt, entry_off, T + 1);
@@ -1153,12 +1209,14 @@ dl_status run(dl_session &s, dl_progress *progress) {
     unsigned long long *pl_scan = P.get<unsigned long long>("pl_scan", T + 1);
     k_tri_words<<<grid_for(T + 1), kBlock, 0, st>>>(sc, tri_off, pair_light, keep, tri_crop, stride, ld_words,
                                                     pl_words);
+    LAUNCHED("k_tri_words");
     ++s.launches;
     scan_u64(s, ld_words, ld_scan, T + 1);
     scan_u64(s, pl_words, pl_scan, T + 1);
     unsigned long long *mesh_words = P.get<unsigned long long>("mesh_words", M + 1);
     unsigned long long *mesh_base = P.get<unsigned long long>("mesh_base", M + 1);
     k_mesh_words<<<grid_for(M + 1), kBlock, 0, st>>>(sc, ld_scan, pl_scan, mesh_words);
+    LAUNCHED("k_mesh_words");
     ++s.launches;
     scan_u64(s, mesh_words, mesh_base, M + 1);
     const unsigned long long total_words = read_back(s, mesh_base + M);
@@ -1168,11 +1226,13 @@ dl_status run(dl_session &s, dl_progress *progress) {
     if (T) {
         k_serialize<<<grid_for(T), kBlock, 0, st>>>(sc, tri_off, pair_light, keep, tri_crop, stride, ld_scan, pl_scan,
                                                     mesh_base, entry_off, words, entry_pair, entry_dst);
+        LAUNCHED("k_serialize");
         ++s.launches;
     }
     if (kept) {
         k_crop<<<grid_for((size_t)kept * 32), kBlock, 0, st>>>(sc, kept, entry_pair, entry_dst, pair_tri, pair_light,
                                                                tri_crop, region_rect, region_off, region_pool, words);
+        LAUNCHED("k_crop");
         ++s.launches;
     }
     CK(cudaEventRecord(e1, st));
@@ -1190,6 +1250,8 @@ dl_status run(dl_session &s, dl_progress *progress) {
     s.report.burial_rays = s.counters.burial_rays;
     s.report.bounce_rays = s.counters.bounce_rays;
     s.report.photon_rays = s.counters.photon_rays;
+    s.report.node_visits = s.counters.node_visits;
+    s.report.tri_tests = s.counters.tri_tests;
     s.report.kernel_launches = s.launches;
     s.report.device_bytes = s.scene_bytes + P.bytes;
     s.out_words = total_words;

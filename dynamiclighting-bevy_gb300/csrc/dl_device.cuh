@@ -100,6 +100,12 @@ struct Hit {
     uint32_t occluder;
 };
 
+// Node visits and triangle tests of traversals, counted only in the instrumented kernel variant
+// the benchmark uses for its roofline bytes.
+struct Visits {
+    unsigned long long nodes, tris;
+};
+
 constexpr int kStack = 64;  // >= BVH depth; the host refuses deeper trees
 
 // Slab test of both children of a node against the ray [0, tmax]. Boxes are padded on the host
@@ -133,8 +139,9 @@ __device__ __forceinline__ f3 safe_inv(f3 d) {
 // memory, slots `stride` apart. For closest-hit, `hit` gets the nearest t (ties to the lowest
 // occluder index, as occluder.rs:205-210) and that test's barycentrics, which equal the ones
 // the reference recomputes with max = infinity.
-template <bool ANY>
-__device__ bool traverse(const DevScene &sc, f3 o, f3 dir, float max, bool alpha, int *stack, int stride, Hit &hit) {
+template <bool ANY, bool COUNT = false>
+__device__ bool traverse(const DevScene &sc, f3 o, f3 dir, float max, bool alpha, int *stack, int stride, Hit &hit,
+                         Visits *vis = nullptr) {
     hit.t = INFINITY;
     hit.u = hit.v = 0.0f;
     hit.occluder = 0xFFFFFFFFu;
@@ -150,6 +157,7 @@ __device__ bool traverse(const DevScene &sc, f3 o, f3 dir, float max, bool alpha
         if (ref >= 0) {
             const float4 *nd = sc.nodes + (size_t)ref * 4;
             float4 a = ldg4(nd), b = ldg4(nd + 1), c = ldg4(nd + 2), r = ldg4(nd + 3);
+            if (COUNT) ++vis->nodes;
             bool h0, h1;
             float n0, n1;
             box2(a, b, c, inv, oinv, ANY ? tmax : fminf(tmax, hit.t), h0, h1, n0, n1);
@@ -173,6 +181,7 @@ __device__ bool traverse(const DevScene &sc, f3 o, f3 dir, float max, bool alpha
             for (uint32_t k = 0; k < count; ++k) {
                 uint32_t i = first + k;
                 float4 v0 = ldg4(sc.tri_v0 + i);
+                if (COUNT) ++vis->tris;
                 float t, u, v;
                 if (!tri_test(v0, ldg4(sc.tri_e1 + i), ldg4(sc.tri_e2 + i), o, d, max, t, u, v)) continue;
                 uint32_t occ = __float_as_uint(v0.w);
@@ -193,10 +202,11 @@ __device__ bool traverse(const DevScene &sc, f3 o, f3 dir, float max, bool alpha
     }
 }
 
+template <bool COUNT = false>
 __device__ __forceinline__ bool occluded(const DevScene &sc, f3 o, f3 d, float max, bool alpha, int *stack,
-                                         int stride) {
+                                         int stride, Visits *vis = nullptr) {
     Hit h;
-    return traverse<true>(sc, o, d, max, alpha, stack, stride, h);
+    return traverse<true, COUNT>(sc, o, d, max, alpha, stack, stride, h, vis);
 }
 
 }  // namespace dl

@@ -174,14 +174,16 @@ struct Vis {
     uint32_t rays;
 };
 
+template <bool COUNT = false>
 struct Tracer {
     const DevScene &sc;
     f3 origin;
     bool alpha;
     int *stack;
     int stride;
+    Visits *vis;
     __device__ __forceinline__ bool operator()(f3 dir, float dist) const {
-        return occluded(sc, origin, dir, dist, alpha, stack, stride);
+        return occluded<COUNT>(sc, origin, dir, dist, alpha, stack, stride, vis);
     }
 };
 
@@ -223,7 +225,8 @@ __device__ __forceinline__ bool adaptive_share(const f2 *probes, int nprobes, ui
 }
 
 // point_texel (texel_shadow.rs:71-90)
-__device__ __forceinline__ Vis point_vis(const DevLight &l, f3 pos, f3 nrm, const Tracer &tr) {
+template <class TR>
+__device__ __forceinline__ Vis point_vis(const DevLight &l, f3 pos, f3 nrm, const TR &tr) {
     f3 to = sub(l.position, pos);
     float dsq = length_sq(to);
     if (dsq > l.radius * l.radius) return Vis{false, 0, 0};
@@ -235,8 +238,9 @@ __device__ __forceinline__ Vis point_vis(const DevLight &l, f3 pos, f3 nrm, cons
 }
 
 // texel_visibility (area.rs:61-90) with toward (area.rs:130-146)
+template <class TR>
 __device__ __forceinline__ Vis area_vis(const DevScene &sc, const DevLight &l, f3 pos, f3 nrm, Pcg &rng,
-                                        const Tracer &tr) {
+                                        const TR &tr) {
     bool rect = l.flags & kLightRect;
     f3 local = sub(pos, l.position);
     float lx = clampf(dot(local, l.ax), -l.half_x, l.half_x);
@@ -274,7 +278,8 @@ __device__ __forceinline__ Vis area_vis(const DevScene &sc, const DevLight &l, f
 }
 
 // sun_visibility (sun.rs:21-56)
-__device__ __forceinline__ Vis sun_vis(const DevScene &sc, const DevLight &l, f3 nrm, Pcg &rng, const Tracer &tr) {
+template <class TR>
+__device__ __forceinline__ Vis sun_vis(const DevScene &sc, const DevLight &l, f3 nrm, Pcg &rng, const TR &tr) {
     if (l.angular_radius <= 0.0f) {
         if (dot(nrm, l.toward) <= kNdotlTolerance) return Vis{false, 0, 0};
         bool lit = !tr(l.toward, INFINITY);
@@ -303,7 +308,8 @@ __device__ __forceinline__ Vis sun_vis(const DevScene &sc, const DevLight &l, f3
 }
 
 // sky_visibility (sky.rs:30-44)
-__device__ __forceinline__ Vis sky_vis(const DevScene &sc, const DevLight &l, f3 nrm, Pcg &rng, const Tracer &tr) {
+template <class TR>
+__device__ __forceinline__ Vis sky_vis(const DevScene &sc, const DevLight &l, f3 nrm, Pcg &rng, const TR &tr) {
     f2 off;
     off.x = rng.next_f32();
     off.y = rng.next_f32();
@@ -316,8 +322,9 @@ __device__ __forceinline__ Vis sky_vis(const DevScene &sc, const DevLight &l, f3
 }
 
 // texel_shadow (texel_shadow.rs:20-67)
+template <class TR>
 __device__ __forceinline__ Vis texel_shadow(const DevScene &sc, uint32_t slot, uint64_t mesh_id, uint32_t x,
-                                            uint32_t y, f3 pos, f3 nrm, const Tracer &tr) {
+                                            uint32_t y, f3 pos, f3 nrm, const TR &tr) {
     const DevLight &l = sc.lights[slot];
     if (l.shape == DL_SHAPE_POINT) return point_vis(l, pos, nrm, tr);
     Pcg rng = stream5(sc.seed, mesh_id, l.id, x, y);

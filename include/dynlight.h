@@ -139,7 +139,8 @@ typedef struct dl_progress {
 enum {
     DL_FORM_BATCHED = 0, /* every (triangle, light) pair through one persistent kernel fed by a
                             device work queue, launched from a CUDA graph */
-    DL_FORM_PLAIN = 1    /* one launch per (mesh, light): the reference's loop order on the GPU */
+    DL_FORM_PLAIN = 1    /* one launch per mesh, a warp per triangle looping over its lights and
+                            texels: the reference's loop order on the GPU */
 };
 
 /* Launch configuration of one bake; zero-initialise for the defaults. */
@@ -150,7 +151,9 @@ typedef struct dl_bake_config {
     uint32_t chunk_texels;     /* texels per work item of the batched queue, 0: default */
     uint32_t sample_lanes;     /* lanes sharing one texel's soft/sky samples, 0: default */
     uint32_t blocks_per_sm;    /* persistent blocks per SM, 0: default */
-    uint32_t reserved[8];
+    uint32_t count_visits;     /* 1: run the instrumented visibility kernel that counts BVH node
+                                  visits and triangle tests (for roofline accounting; slower) */
+    uint32_t reserved[7];
 } dl_bake_config;
 
 /* Timings (device events, milliseconds) and counters of the last bake. */
@@ -172,6 +175,8 @@ typedef struct dl_bake_report {
     uint64_t h2d_bytes;
     uint64_t d2h_bytes;
     uint64_t device_bytes;    /* peak device memory held by the bake */
+    uint64_t node_visits;     /* BVH nodes visited by the visibility stage (counting config only) */
+    uint64_t tri_tests;       /* triangle tests of the visibility stage (counting config only) */
 } dl_bake_report;
 
 /* LightBvhNode (src/bake/light_bvh.rs:16-22), 32 bytes. */
