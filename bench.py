@@ -180,11 +180,6 @@ def main():
     session = dl.Session(inp, opts, form="batched", device=local)
     for _ in range(args.warmup):
         session.run()
-    plain = dl.Session(inp, opts, form="plain", device=local)
-    plain.run()
-    plain_rep = plain.report()
-    plain_result = plain.result()
-    plain.close()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -199,6 +194,12 @@ def main():
     torch.cuda.synchronize()
     result = session.result()
     rep = session.report()
+    # the plain form (one launch per mesh), same scene, for the batched/plain ratio
+    plain = dl.Session(inp, opts, form="plain", device=local)
+    plain.run()
+    plain_rep = plain.report()
+    plain_result = plain.result()
+    plain.close()
     rays = result.stats["rays"] + result.stats["bounce_rays"]
     ms = statistics.median(dev_ms)
     t_max = ms
@@ -255,7 +256,9 @@ def main():
         "clocks": clocks.summary(),
         "gpu_launches": int(rep.kernel_launches),
         "e2e": {"value": e2e_value, "unit": "rays/s", "ms": statistics.median(e2e_ms),
-                "h2d_bytes_per_step": int(e2e_rep.h2d_bytes), "d2h_bytes_per_step": int(e2e_rep.d2h_bytes)},
+                "h2d_bytes_per_step": int(e2e_rep.h2d_bytes), "d2h_bytes_per_step": int(e2e_rep.d2h_bytes),
+                "ms_prepare_bvh_upload": e2e_rep.ms_upload, "ms_device": e2e_rep.ms_device,
+                "ms_download_serialize": e2e_rep.ms_download},
         "roofline": {"bound": "hbm", "kernel": "k_trace_batched", "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "traffic": traffic, "algorithmic_bytes_per_launch": int(alg_bytes),

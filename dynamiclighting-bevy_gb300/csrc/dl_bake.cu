@@ -421,6 +421,287 @@ __global__ void k_item_counts(const uint32_t *order, const uint32_t *pair_tri, c
     cnt[i] = ctex_off[t + 1] - ctex_off[t];
 }
 
+
+// ================================ one bounce ===========================================
+
+// PhotonCube::build (bounce.rs:48-70): every cube texel of every local bounce light.
+__global__ void __launch_bounds__(kBlock) k_photons(DevScene sc, const uint32_t *cube_lights, uint32_t cubes,
+                                                    uint32_t res, Photon *photons) {
+    __shared__ int stack[kStack * kBlock];
+    uint64_t per = 6ull * res * res;
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= per * cubes) return;
+    uint32_t cube = (uint32_t)(i / per);
+    uint32_t rem = (uint32_t)(i % per);
+    uint32_t face = rem / (res * res), y = (rem % (res * res)) / res, x = rem % res;
+    const DevLight &l = sc.lights[cube_lights[cube]];
+    photons[i] = make_photon(sc, l, cube_texel_direction(face, x, y, res), stack + threadIdx.x, kBlock);
+}
+
+// Pairs whose light bakes bounce, in pair order.
+__global__ void k_bounce_flag(DevScene sc, const uint32_t *pair_light, uint32_t pairs, uint32_t *flag) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p > pairs) return;
+    flag[p] = p < pairs && (sc.lights[pair_light[p]].flags & kLightBounce) ? 1u : 0u;
+}
+
+struct BounceArgs {
+    const uint32_t *pair_tri, *pair_light;
+    const uint32_t *ctex_off, *ctex_xy;
+    const float4 *ctex_pos, *tri_face;
+    const uint32_t *bpairs, *bitem_off;
+    uint32_t bpair_count;
+    unsigned long long items;
+    const Photon *photons;
+    uint32_t res;
+    float4 *value;  // xyz: gathered value, w: 1 when gathered
+    Counters *ctr;
+};
+
+// gather_triangle / gather_sun (bounce.rs:235-292, sun_bounce.rs:24-80): one thread per
+// (bounce pair, texel).
+__global__ void __launch_bounds__(kBlock) k_gather(DevScene sc, BounceArgs a) {
+    __shared__ int stack[kStack * kBlock];
+    int *my = stack + threadIdx.x;
+    unsigned long long rays = 0;
+    unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long item = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; item < a.items;
+         item += stride) {
+        uint32_t lo = 0, hi = a.bpair_count;
+        while (hi - lo > 1) {
+            uint32_t mid = (lo + hi) >> 1;
+            if ((unsigned long long)a.bitem_off[mid] <= item) lo = mid;
+            else hi = mid;
+        }
+        uint32_t p = a.bpairs[lo];
+        uint32_t t = a.pair_tri[p], s = a.pair_light[p];
+        uint32_t m = sc.tri_mesh[t];
+        uint32_t ci = a.ctex_off[t] + (uint32_t)(item - a.bitem_off[lo]);
+        uint32_t xy = a.ctex_xy[ci];
+        float4 pp = a.ctex_pos[ci], f = a.tri_face[t];
+        f3 pos{pp.x, pp.y, pp.z}, normal{f.x, f.y, f.z};
+        f3 origin = add(pos, scale(normal, kRayOffset));
+        const DevLight &l = sc.lights[s];
+        f3 v{0.0f, 0.0f, 0.0f};
+        uint32_t r = 0;
+        bool gathered = true;
+        if (l.shape == DL_SHAPE_SUN) {
+            gather_sun(sc, l, sc.mesh_id[m], xy & 0xFFFFu, xy >> 16, origin, normal, my, kBlock, v, r);
+        } else {
+            Tracer<false> tr{sc, origin, (l.flags & kLightAlpha) != 0, my, kBlock, nullptr};
+            gathered = gather_local(sc, l, a.photons + (size_t)l.cube * 6 * a.res * a.res, a.res, sc.mesh_id[m],
+                                    xy & 0xFFFFu, xy >> 16, pos, normal, tr, v, r);
+        }
+        rays += r;
+        a.value[item] = make_float4(v.x, v.y, v.z, gathered ? 1.0f : 0.0f);
+    }
+    unsigned long long sum = warp_sum(rays);
+    if (lane_id() == 0 && sum) atomicAdd(&a.ctr->bounce_rays, sum);
+}
+
+// The bounce window of a (mesh, light) entry: its crops' union grown by 4 (bounce_map.rs:30-43).
+__device__ __forceinline__ Rect bounce_window(const uint32_t *r, uint32_t res) {
+    uint32_t last = res - 1;
+    return Rect{r[0] >= 4 ? r[0] - 4 : 0, r[1] >= 4 ? r[1] - 4 : 0, min(r[2] + 4, last), min(r[3] + 4, last)};
+}
+
+__global__ void k_window_sizes(DevScene sc, const uint32_t *region_rect, uint32_t entries, uint32_t *size) {
+    uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e > entries) return;
+    size[e] = 0;
+    if (e == entries) return;
+    const uint32_t *r = region_rect + (size_t)e * 4;
+    uint32_t s = e % sc.light_count, m = e / sc.light_count;
+    if (r[0] == kNoRect || !(sc.lights[s].flags & kLightBounce)) return;
+    Rect w = bounce_window(r, sc.mesh_res[m]);
+    size[e] = (w.max_x - w.min_x + 1) * (w.max_y - w.min_y + 1);
+}
+
+// Later triangles overwrite shared texels (bounce.rs:202-209): the highest triangle index that
+// gathered a texel owns it; a second pass writes the owner's value.
+template <bool WRITE>
+__global__ void k_bounce_scatter(DevScene sc, BounceArgs a, const uint32_t *region_rect, const uint32_t *woff,
+                                 uint32_t *owner, float4 *map) {
+    unsigned long long item = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= a.items) return;
+    float4 v = a.value[item];
+    if (v.w == 0.0f) return;
+    uint32_t lo = 0, hi = a.bpair_count;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if ((unsigned long long)a.bitem_off[mid] <= item) lo = mid;
+        else hi = mid;
+    }
+    uint32_t p = a.bpairs[lo];
+    uint32_t t = a.pair_tri[p], s = a.pair_light[p];
+    uint32_t m = sc.tri_mesh[t];
+    size_t e = (size_t)m * sc.light_count + s;
+    Rect w = bounce_window(region_rect + e * 4, sc.mesh_res[m]);
+    uint32_t xy = a.ctex_xy[a.ctex_off[t] + (uint32_t)(item - a.bitem_off[lo])];
+    uint32_t x = xy & 0xFFFFu, y = xy >> 16;
+    size_t idx = woff[e] + (size_t)(y - w.min_y) * (w.max_x - w.min_x + 1) + (x - w.min_x);
+    uint32_t key = t - sc.mesh_tri_base[m] + 1;
+    if (!WRITE)
+        atomicMax(owner + idx, key);
+    else if (owner[idx] == key)
+        map[idx] = make_float4(v.x, v.y, v.z, 0.0f);
+}
+
+// dilate then separable blur (bounce_map.rs:67-112) of one window per block; A holds the
+// scattered map on entry and B the filtered map on exit.
+__global__ void __launch_bounds__(256) k_bounce_filter(DevScene sc, const uint32_t *region_rect, const uint32_t *woff,
+                                                       const uint32_t *wsize, float4 *A, float4 *B, float w0, float w1,
+                                                       float w2, float w3, float w4, float w5, float w6, float wsum) {
+    size_t e = blockIdx.x;
+    if (!wsize[e]) return;
+    uint32_t m = (uint32_t)(e / sc.light_count);
+    uint32_t res = sc.mesh_res[m];
+    Rect w = bounce_window(region_rect + e * 4, res);
+    uint32_t ww = w.max_x - w.min_x + 1, wh = w.max_y - w.min_y + 1, n = ww * wh;
+    float4 *a = A + woff[e], *b = B + woff[e];
+    auto get = [&](const float4 *g, int64_t x, int64_t y) -> float4 {
+        if (x < (int64_t)w.min_x || y < (int64_t)w.min_y || x > (int64_t)w.max_x || y > (int64_t)w.max_y)
+            return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return g[(size_t)(y - w.min_y) * ww + (x - w.min_x)];
+    };
+    const int order[9][2] = {{0, 0}, {-1, -1}, {0, -1}, {1, -1}, {-1, 0}, {1, 0}, {-1, 1}, {0, 1}, {1, 1}};
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        int64_t x = w.min_x + i % ww, y = w.min_y + i / ww;
+        float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (int k = 0; k < 9; ++k) {
+            float4 v = get(a, x + order[k][0], y + order[k][1]);
+            if (fmaxf(fmaxf(v.x, v.y), v.z) > 0.0f) {
+                out = v;
+                break;
+            }
+        }
+        b[i] = out;
+    }
+    __syncthreads();
+    const float wt[7] = {w0, w1, w2, w3, w4, w5, w6};
+    int64_t last = (int64_t)res - 1;
+    for (int pass = 0; pass < 2; ++pass) {
+        const float4 *src = pass == 0 ? b : a;
+        float4 *dst = pass == 0 ? a : b;
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+            int64_t x = w.min_x + i % ww, y = w.min_y + i / ww;
+            float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+            for (int k = -3; k <= 3; ++k) {
+                int64_t qx = pass == 0 ? min(max(x + k, (int64_t)0), last) : x;
+                int64_t qy = pass == 0 ? y : min(max(y + k, (int64_t)0), last);
+                float4 v = get(src, qx, qy);
+                sx = sx + v.x * wt[k + 3];
+                sy = sy + v.y * wt[k + 3];
+                sz = sz + v.z * wt[k + 3];
+            }
+            dst[i] = make_float4(sx / wsum, sy / wsum, sz / wsum, 0.0f);
+        }
+        __syncthreads();
+    }
+}
+
+// BounceMap::crop's "lit" test (bounce_map.rs:124-136) per bounce pair: a warp scans the
+// triangle's crop in the filtered window.
+__global__ void k_bounce_lit(DevScene sc, BounceArgs a, const uint4 *tri_crop, const uint32_t *region_rect,
+                             const uint32_t *woff, const float4 *map, uint8_t *pair_bounce) {
+    uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    unsigned lane = lane_id();
+    if (b >= a.bpair_count) return;
+    uint32_t p = a.bpairs[b];
+    uint32_t t = a.pair_tri[p], s = a.pair_light[p];
+    uint32_t m = sc.tri_mesh[t];
+    size_t e = (size_t)m * sc.light_count + s;
+    Rect w = bounce_window(region_rect + e * 4, sc.mesh_res[m]);
+    uint32_t ww = w.max_x - w.min_x + 1;
+    uint4 c = tri_crop[t];
+    uint32_t cw = c.z - c.x + 1;
+    uint64_t n = (uint64_t)cw * (c.w - c.y + 1);
+    bool lit = false;
+    for (uint64_t base = 0; base < n && !lit; base += 32) {
+        uint64_t i = base + lane;
+        bool l = false;
+        if (i < n) {
+            uint32_t x = c.x + (uint32_t)(i % cw), y = c.y + (uint32_t)(i / cw);
+            float4 v = map[woff[e] + (size_t)(y - w.min_y) * ww + (x - w.min_x)];
+            l = fmaxf(fmaxf(v.x, v.y), v.z) > 0.0f;
+        }
+        lit = __any_sync(0xFFFFFFFFu, l);
+    }
+    if (lane == 0) pair_bounce[p] = lit;
+}
+
+__device__ __forceinline__ uint64_t bounce_words(uint4 crop, uint32_t bits, bool colored) {
+    uint64_t n = (uint64_t)(crop.z - crop.x + 5) * (crop.w - crop.y + 5);
+    if (colored) return (n * 3 * bits + 31) / 32;
+    uint32_t per = 32 / bits;
+    return (n + per - 1) / per;
+}
+
+// pack_bounce / pack_bounce_rgb (bounce_pack.rs:28-71) of one kept entry: the padded crop grid
+// of the filtered map, dithered from the stream [seed, mesh, light, triangle] in texel order.
+__global__ void k_pack_bounce(DevScene sc, uint32_t entries, const uint32_t *entry_pair,
+                              const unsigned long long *entry_bdst, const uint32_t *pair_tri,
+                              const uint32_t *pair_light, const uint4 *tri_crop, const uint32_t *region_rect,
+                              const uint32_t *woff, const float4 *map, uint32_t *words) {
+    uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= entries) return;
+    unsigned long long dst = entry_bdst[e];
+    if (dst == ~0ull) return;
+    uint32_t p = entry_pair[e];
+    uint32_t t = pair_tri[p], s = pair_light[p];
+    uint32_t m = sc.tri_mesh[t];
+    const DevLight &l = sc.lights[s];
+    size_t re = (size_t)m * sc.light_count + s;
+    Rect w = bounce_window(region_rect + re * 4, sc.mesh_res[m]);
+    uint32_t ww = w.max_x - w.min_x + 1;
+    uint4 c = tri_crop[t];
+    int gw = (int)(c.z - c.x + 5), gh = (int)(c.w - c.y + 5);
+    uint32_t bits = l.bounce_bits;
+    Pcg rng = stream4(sc.seed, sc.mesh_id[m], l.id, t - sc.mesh_tri_base[m]);
+    bool colored = sc.colored_bounce != 0;
+    uint32_t pixel_bits = colored ? 3 * bits : bits;
+    uint32_t per = 32 / bits;
+    unsigned long long acc = 0;  // bits not yet written
+    uint32_t acc_bits = 0;
+    uint64_t out = dst;
+    uint64_t n = (uint64_t)gw * gh;
+    for (uint64_t i = 0; i < n; ++i) {
+        int gx = (int)(i % gw), gy = (int)(i / gw);
+        float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (gx >= 2 && gy >= 2 && gx < gw - 2 && gy < gh - 2) {
+            uint32_t x = c.x + gx - 2, y = c.y + gy - 2;
+            v = map[woff[re] + (size_t)(y - w.min_y) * ww + (x - w.min_x)];
+        }
+        uint32_t pixel;
+        if (colored) {
+            pixel = quantize_bounce(v.x, bits, rng);
+            pixel |= quantize_bounce(v.y, bits, rng) << bits;
+            pixel |= quantize_bounce(v.z, bits, rng) << (2 * bits);
+        } else {
+            pixel = quantize_bounce(v.x, bits, rng);
+        }
+        if (colored) {
+            // one bit stream, pixels 3*bits wide
+            acc |= (unsigned long long)pixel << acc_bits;
+            acc_bits += pixel_bits;
+            while (acc_bits >= 32) {
+                words[out++] = (uint32_t)acc;
+                acc >>= 32;
+                acc_bits -= 32;
+            }
+        } else {
+            // floor(32 / bits) pixels per word, the rest of each word left zero
+            uint32_t j = (uint32_t)(i % per);
+            acc |= (unsigned long long)pixel << (j * bits);
+            if (j == per - 1) {
+                words[out++] = (uint32_t)acc;
+                acc = 0;
+            }
+        }
+    }
+    if (colored ? acc_bits > 0 : (n % per) != 0) words[out++] = (uint32_t)acc;
+}
+
 // ================================ optimize, seams, serialize ===========================
 
 __device__ __forceinline__ uint32_t region_get(const uint32_t *pool, uint32_t off, const uint32_t *r, uint32_t bits,
@@ -432,40 +713,47 @@ __device__ __forceinline__ uint32_t region_get(const uint32_t *pool, uint32_t of
     return (pool[off + idx / 4] >> ((idx % 4) * 8)) & 0xFFu;
 }
 
-// LightEntries::optimize (shadows.rs:54-73) + any_light (:136-144); marks used regions.
-__global__ void k_optimize(DevScene sc, const uint32_t *tri_off, const uint32_t *pair_light,
+// LightEntries::optimize (shadows.rs:54-73) + any_light (:136-144): a warp per pair scans the
+// triangle's optimize rect within the light's region for any lit texel; marks used regions and
+// counts kept entries per triangle.
+__global__ void k_optimize(DevScene sc, uint32_t pairs, const uint32_t *pair_tri, const uint32_t *pair_light,
                            const uint32_t *region_rect, const uint32_t *region_off, const uint32_t *region_pool,
                            const uint8_t *pair_bounce, uint8_t *keep, uint32_t *kept_count, uint8_t *used,
                            Counters *ctr) {
-    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= sc.triangles) return;
+    uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    unsigned lane = lane_id();
+    if (p >= pairs) return;
+    uint32_t t = pair_tri[p], s = pair_light[p];
     TriData d;
     load_tri(sc, t, d);
-    Rect o = center_rect(d.uv, d.res, 1.0f);
-    uint32_t kept = 0, removed = 0;
-    for (uint32_t p = tri_off[t]; p < tri_off[t + 1]; ++p) {
-        uint32_t s = pair_light[p];
-        size_t e = (size_t)d.mesh * sc.light_count + s;
-        bool k = pair_bounce && pair_bounce[p];
-        if (!k) {
-            const uint32_t *r = region_rect + e * 4;
-            uint32_t min_x = max(o.min_x, r[0]), max_x = min(o.max_x, r[2]);
-            uint32_t min_y = max(o.min_y, r[1]), max_y = min(o.max_y, r[3]);
-            uint32_t bits = sc.lights[s].shadow_bits;
-            for (uint32_t y = min_y; y <= max_y && !k && min_x <= max_x; ++y)
-                for (uint32_t x = min_x; x <= max_x && !k; ++x)
-                    k = region_get(region_pool, region_off[e], r, bits, x, y) != 0;
-        }
-        keep[p] = k;
-        if (k) {
-            ++kept;
-            used[e] = 1;
-        } else {
-            ++removed;
+    size_t e = (size_t)d.mesh * sc.light_count + s;
+    bool k = pair_bounce && pair_bounce[p];
+    if (!k) {
+        Rect o = center_rect(d.uv, d.res, 1.0f);
+        const uint32_t *r = region_rect + e * 4;
+        uint32_t min_x = max(o.min_x, r[0]), max_x = min(o.max_x, r[2]);
+        uint32_t min_y = max(o.min_y, r[1]), max_y = min(o.max_y, r[3]);
+        if (min_x <= max_x && min_y <= max_y) {
+            uint32_t w = max_x - min_x + 1;
+            uint64_t n = (uint64_t)w * (max_y - min_y + 1);
+            uint32_t bits = sc.lights[s].shadow_bits, roff = region_off[e];
+            for (uint64_t base = 0; base < n && !k; base += 32) {
+                uint64_t i = base + lane;
+                bool lit = i < n && region_get(region_pool, roff, r, bits, min_x + (uint32_t)(i % w),
+                                               min_y + (uint32_t)(i / w)) != 0;
+                k = __any_sync(0xFFFFFFFFu, lit);
+            }
         }
     }
-    kept_count[t] = kept;
-    if (removed) atomicAdd(&ctr->lights_removed, (unsigned long long)removed);
+    if (lane == 0) {
+        keep[p] = k;
+        if (k) {
+            used[e] = 1;
+            atomicAdd(kept_count + t, 1u);
+        } else {
+            atomicAdd(&ctr->lights_removed, 1ull);
+        }
+    }
 }
 
 // pad_seams (seams.rs:15-39) on every used region; a block per (mesh, light) entry.
@@ -513,8 +801,8 @@ __device__ __forceinline__ uint64_t shadow_words(uint4 crop, uint32_t bits) {
 
 // Words per triangle: light data (1 + stride per kept light) and payload.
 __global__ void k_tri_words(DevScene sc, const uint32_t *tri_off, const uint32_t *pair_light, const uint8_t *keep,
-                            const uint4 *tri_crop, uint32_t stride, unsigned long long *ld_words,
-                            unsigned long long *pl_words) {
+                            const uint8_t *pair_bounce, const uint4 *tri_crop, uint32_t stride,
+                            unsigned long long *ld_words, unsigned long long *pl_words) {
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t > sc.triangles) return;
     if (t == sc.triangles) {
@@ -525,8 +813,10 @@ __global__ void k_tri_words(DevScene sc, const uint32_t *tri_off, const uint32_t
     unsigned long long ld = 1, pl = 0;
     for (uint32_t p = tri_off[t]; p < tri_off[t + 1]; ++p)
         if (keep[p]) {
+            const DevLight &l = sc.lights[pair_light[p]];
             ld += stride;
-            pl += shadow_words(c, sc.lights[pair_light[p]].shadow_bits);
+            pl += shadow_words(c, l.shadow_bits);
+            if (stride == 3 && pair_bounce[p]) pl += bounce_words(c, l.bounce_bits, sc.colored_bounce != 0);
         }
     ld_words[t] = ld;
     pl_words[t] = pl;
@@ -547,10 +837,10 @@ __global__ void k_mesh_words(DevScene sc, const unsigned long long *ld_scan, con
 // serialize_triangles (triangle_words.rs:47-89): headers, light data, and where each kept
 // entry's shadow words go.
 __global__ void k_serialize(DevScene sc, const uint32_t *tri_off, const uint32_t *pair_light, const uint8_t *keep,
-                            const uint4 *tri_crop, uint32_t stride, const unsigned long long *ld_scan,
-                            const unsigned long long *pl_scan, const unsigned long long *mesh_base,
-                            const uint32_t *entry_off, uint32_t *words, uint32_t *entry_pair,
-                            unsigned long long *entry_dst) {
+                            const uint8_t *pair_bounce, const uint4 *tri_crop, uint32_t stride,
+                            const unsigned long long *ld_scan, const unsigned long long *pl_scan,
+                            const unsigned long long *mesh_base, const uint32_t *entry_off, uint32_t *words,
+                            uint32_t *entry_pair, unsigned long long *entry_dst, unsigned long long *entry_bdst) {
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= sc.triangles) return;
     uint32_t m = sc.tri_mesh[t];
@@ -570,13 +860,22 @@ __global__ void k_serialize(DevScene sc, const uint32_t *tri_off, const uint32_t
     for (uint32_t p = tri_off[t]; p < tri_off[t + 1]; ++p) {
         if (!keep[p]) continue;
         uint32_t s = pair_light[p];
+        const DevLight &l = sc.lights[s];
         uint32_t at = ld + 1 + count * stride;
         words[base + at] = s;
         words[base + at + 1] = pl;
-        if (stride == 3) words[base + at + 2] = 0;
         entry_pair[e] = p;
         entry_dst[e] = base + pl;
-        pl += (uint32_t)shadow_words(c, sc.lights[s].shadow_bits);
+        pl += (uint32_t)shadow_words(c, l.shadow_bits);
+        entry_bdst[e] = ~0ull;
+        if (stride == 3) {
+            words[base + at + 2] = 0;
+            if (pair_bounce[p]) {
+                words[base + at + 2] = pl;
+                entry_bdst[e] = base + pl;
+                pl += (uint32_t)bounce_words(c, l.bounce_bits, sc.colored_bounce != 0);
+            }
+        }
         ++count;
         ++e;
     }
@@ -618,13 +917,18 @@ __device__ __forceinline__ uint32_t crop_level(const uint32_t *pool, uint32_t of
     return in_ring ? inner(gx, gy) : interior(gx, gy);
 }
 
-__global__ void k_crop(DevScene sc, uint32_t entries, const uint32_t *entry_pair, const unsigned long long *entry_dst,
-                       const uint32_t *pair_tri, const uint32_t *pair_light, const uint4 *tri_crop,
-                       const uint32_t *region_rect, const uint32_t *region_off, const uint32_t *region_pool,
-                       uint32_t *words) {
+constexpr int kCropBytes = 2048;  // per-warp staging grid in shared memory (texels)
+
+__global__ void __launch_bounds__(kBlock) k_crop(DevScene sc, uint32_t entries, const uint32_t *entry_pair,
+                                                const unsigned long long *entry_dst, const uint32_t *pair_tri,
+                                                const uint32_t *pair_light, const uint4 *tri_crop,
+                                                const uint32_t *region_rect, const uint32_t *region_off,
+                                                const uint32_t *region_pool, uint32_t *words) {
+    __shared__ uint8_t stage[kBlock / 32][kCropBytes];
     uint32_t e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     unsigned lane = lane_id();
     if (e >= entries) return;
+    uint8_t *g = stage[threadIdx.x >> 5];
     uint32_t p = entry_pair[e];
     uint32_t t = pair_tri[p], s = pair_light[p];
     uint32_t m = sc.tri_mesh[t];
@@ -638,12 +942,61 @@ __global__ void k_crop(DevScene sc, uint32_t entries, const uint32_t *entry_pair
     uint32_t per = 32 / bits;
     uint64_t nw = (n + per - 1) / per;
     unsigned long long dst = entry_dst[e];
+    if (n > (uint64_t)kCropBytes) {
+        // large crops: every texel straight from the region
+        for (uint64_t wi = lane; wi < nw; wi += 32) {
+            uint32_t word = 0;
+            for (uint32_t j = 0; j < per; ++j) {
+                uint64_t i = wi * per + j;
+                if (i >= n) break;
+                uint32_t v = crop_level(region_pool, off, r, bits, c, gw, gh, (int)(i % gw), (int)(i / gw));
+                word |= (bits == 1 ? (v != 0) : v) << (j * bits);
+            }
+            words[dst + wi] = word;
+        }
+        return;
+    }
+    auto interior = [&](int x, int y) { return x >= 2 && y >= 2 && x < gw - 2 && y < gh - 2; };
+    auto outer = [&](int x, int y) { return x == 0 || y == 0 || x == gw - 1 || y == gh - 1; };
+    // the crop: interior texels from the region, padding rings zero
+    for (int i = lane; i < (int)n; i += 32) {
+        int x = i % gw, y = i / gw;
+        g[i] = interior(x, y) ? (uint8_t)region_get(region_pool, off, r, bits, (int64_t)c.x + x - 2,
+                                                     (int64_t)c.y + y - 2)
+                              : 0;
+    }
+    __syncwarp();
+    // first ring pass: inner ring = 3x3 max of the crop (only interior texels are non-zero there)
+    for (int i = lane; i < (int)n; i += 32) {
+        int x = i % gw, y = i / gw;
+        if (interior(x, y) || outer(x, y)) continue;
+        uint32_t v = 0;
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx)
+                if (interior(x + dx, y + dy)) v = max(v, (uint32_t)g[(y + dy) * gw + x + dx]);
+        g[i] = (uint8_t)v;
+    }
+    __syncwarp();
+    // second ring pass: outer ring = 3x3 max of interior and inner ring (outer cells are 0 then)
+    for (int i = lane; i < (int)n; i += 32) {
+        int x = i % gw, y = i / gw;
+        if (!outer(x, y)) continue;
+        uint32_t v = 0;
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                int xx = x + dx, yy = y + dy;
+                if (xx < 0 || yy < 0 || xx >= gw || yy >= gh || outer(xx, yy)) continue;
+                v = max(v, (uint32_t)g[yy * gw + xx]);
+            }
+        g[i] = (uint8_t)v;
+    }
+    __syncwarp();
     for (uint64_t wi = lane; wi < nw; wi += 32) {
         uint32_t word = 0;
         for (uint32_t j = 0; j < per; ++j) {
             uint64_t i = wi * per + j;
             if (i >= n) break;
-            uint32_t v = crop_level(region_pool, off, r, bits, c, gw, gh, (int)(i % gw), (int)(i / gw));
+            uint32_t v = g[i];
             word |= (bits == 1 ? (v != 0) : v) << (j * bits);
         }
         words[dst + wi] = word;
@@ -967,6 +1320,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
     CK(cudaEventRecord(e0, st));
     CK(cudaMemsetAsync(s.ctr, 0, sizeof(Counters), st));
     CK(cudaMemsetAsync(s.cancel_dev, 0, 4, st));
+    s.report.photon_rays = 0;
     if (T == 0) {
         // no triangles: every mesh serializes to no words (triangle_words.rs:47-56)
         CK(cudaEventRecord(v0, st));
@@ -1179,16 +1533,108 @@ dl_status run(dl_session &s, dl_progress *progress) {
     wait(s, progress);
     if (check_cancel()) return DL_CANCELLED;
 
+    // ---- one bounce: photon cubes, gathers, bounce maps (bounce.rs:48-217)
+    const HostScene &hs = s.host;
+    uint8_t *pair_bounce = P.get<uint8_t>("pair_bounce", pairs);
+    CK(cudaMemsetAsync(pair_bounce, 0, pairs, st));
+    uint32_t *woff = nullptr;
+    float4 *bmap = nullptr;
+    if (hs.bounce_in_scene && pairs) {
+        const uint32_t res = s.options.photon_cube_resolution;
+        const uint32_t cubes = (uint32_t)hs.cube_lights.size();
+        const uint64_t photons_n = 6ull * res * res * cubes;
+        Photon *photons = P.get<Photon>("photons", photons_n);
+        if (cubes) {
+            uint32_t *cube_lights = P.get<uint32_t>("cube_lights", cubes);
+            CK(cudaMemcpyAsync(cube_lights, hs.cube_lights.data(), cubes * 4ull, cudaMemcpyHostToDevice, st));
+            k_photons<<<grid_for(photons_n), kBlock, 0, st>>>(sc, cube_lights, cubes, res, photons);
+            LAUNCHED("k_photons");
+            ++s.launches;
+        }
+        s.report.photon_rays = photons_n;
+        uint32_t *bflag = P.get<uint32_t>("bflag", pairs + 1);
+        uint32_t *bpos = P.get<uint32_t>("bpos", pairs + 1);
+        k_bounce_flag<<<grid_for(pairs + 1), kBlock, 0, st>>>(sc, pair_light, pairs, bflag);
+        LAUNCHED("k_bounce_flag");
+        scan_u32(s, bflag, bpos, pairs + 1);
+        const uint32_t bcount = read_back(s, bpos + pairs);
+        uint32_t *bpairs = P.get<uint32_t>("bpairs", bcount + 1);
+        k_pair_scatter<<<grid_for(pairs), kBlock, 0, st>>>(bflag, bpos, pairs, 0, bpairs);
+        LAUNCHED("k_pair_scatter");
+        uint32_t *bcnt = P.get<uint32_t>("bcnt", bcount + 1);
+        uint32_t *bitem_off = P.get<uint32_t>("bitem_off", bcount + 1);
+        k_item_counts<<<grid_for(bcount + 1), kBlock, 0, st>>>(bpairs, pair_tri, ctex_off, bcount, bcnt);
+        LAUNCHED("k_item_counts");
+        scan_u32(s, bcnt, bitem_off, bcount + 1);
+        const uint32_t bitems = read_back(s, bitem_off + bcount);
+        s.launches += 3;
+        float4 *bval = P.get<float4>("bval", bitems);
+        BounceArgs ba{};
+        ba.pair_tri = pair_tri;
+        ba.pair_light = pair_light;
+        ba.ctex_off = ctex_off;
+        ba.ctex_xy = ctex_xy;
+        ba.ctex_pos = ctex_pos;
+        ba.tri_face = tri_face;
+        ba.bpairs = bpairs;
+        ba.bitem_off = bitem_off;
+        ba.bpair_count = bcount;
+        ba.items = bitems;
+        ba.photons = photons;
+        ba.res = res;
+        ba.value = bval;
+        ba.ctr = s.ctr;
+        if (bitems) {
+            int per_sm = 0;
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather, kBlock, 0));
+            unsigned blocks = (unsigned)std::min<size_t>(grid_for(bitems), (size_t)std::max(1, per_sm) * s.sms * 8);
+            k_gather<<<blocks, kBlock, 0, st>>>(sc, ba);
+            LAUNCHED("k_gather");
+            ++s.launches;
+        }
+        // windows per (mesh, bounce light)
+        uint32_t *wsize = P.get<uint32_t>("wsize", entries + 1);
+        woff = P.get<uint32_t>("woff", entries + 1);
+        k_window_sizes<<<grid_for(entries + 1), kBlock, 0, st>>>(sc, region_rect, (uint32_t)entries, wsize);
+        LAUNCHED("k_window_sizes");
+        scan_u32(s, wsize, woff, entries + 1);
+        const uint32_t wtotal = read_back(s, woff + entries);
+        uint32_t *owner = P.get<uint32_t>("owner", wtotal);
+        float4 *mapA = P.get<float4>("mapA", wtotal);
+        bmap = P.get<float4>("mapB", wtotal);
+        CK(cudaMemsetAsync(owner, 0, wtotal * 4ull, st));
+        CK(cudaMemsetAsync(mapA, 0, wtotal * 16ull, st));
+        if (bitems) {
+            k_bounce_scatter<false><<<grid_for(bitems), kBlock, 0, st>>>(sc, ba, region_rect, woff, owner, mapA);
+            LAUNCHED("k_bounce_scatter");
+            k_bounce_scatter<true><<<grid_for(bitems), kBlock, 0, st>>>(sc, ba, region_rect, woff, owner, mapA);
+            LAUNCHED("k_bounce_scatter");
+            s.launches += 2;
+        }
+        const float *bw = hs.blur_weights;
+        k_bounce_filter<<<(unsigned)entries, 256, 0, st>>>(sc, region_rect, woff, wsize, mapA, bmap, bw[0], bw[1], bw[2],
+                                                           bw[3], bw[4], bw[5], bw[6], hs.blur_weight_sum);
+        LAUNCHED("k_bounce_filter");
+        if (bcount) {
+            k_bounce_lit<<<grid_for((size_t)bcount * 32), kBlock, 0, st>>>(sc, ba, tri_crop, region_rect, woff, bmap,
+                                                                           pair_bounce);
+            LAUNCHED("k_bounce_lit");
+            ++s.launches;
+        }
+        s.launches += 3;
+    }
+
     // ---- optimize, seams
     uint8_t *keep = P.get<uint8_t>("keep", pairs);
     uint32_t *kept_cnt = P.get<uint32_t>("kept_cnt", T + 1);
     uint32_t *entry_off = P.get<uint32_t>("entry_off", T + 1);
     uint8_t *used = P.get<uint8_t>("used", entries);
     CK(cudaMemsetAsync(used, 0, entries, st));
-    CK(cudaMemsetAsync(kept_cnt + T, 0, 4, st));
-    if (T) {
-        k_optimize<<<grid_for(T), kBlock, 0, st>>>(sc, tri_off, pair_light, region_rect, region_off, region_pool,
-                                                   nullptr, keep, kept_cnt, used, s.ctr);
+    CK(cudaMemsetAsync(kept_cnt, 0, (T + 1) * 4ull, st));
+    if (pairs) {
+        k_optimize<<<grid_for((size_t)pairs * 32), kBlock, 0, st>>>(sc, pairs, pair_tri, pair_light, region_rect,
+                                                                    region_off, region_pool, pair_bounce, keep, kept_cnt,
+                                                                    used, s.ctr);
         LAUNCHED("k_optimize");
         ++s.launches;
     }
@@ -1207,8 +1653,8 @@ dl_status run(dl_session &s, dl_progress *progress) {
     unsigned long long *pl_words = P.get<unsigned long long>("pl_words", T + 1);
     unsigned long long *ld_scan = P.get<unsigned long long>("ld_scan", T + 1);
     unsigned long long *pl_scan = P.get<unsigned long long>("pl_scan", T + 1);
-    k_tri_words<<<grid_for(T + 1), kBlock, 0, st>>>(sc, tri_off, pair_light, keep, tri_crop, stride, ld_words,
-                                                    pl_words);
+    k_tri_words<<<grid_for(T + 1), kBlock, 0, st>>>(sc, tri_off, pair_light, keep, pair_bounce, tri_crop, stride,
+                                                    ld_words, pl_words);
     LAUNCHED("k_tri_words");
     ++s.launches;
     scan_u64(s, ld_words, ld_scan, T + 1);
@@ -1223,9 +1669,11 @@ dl_status run(dl_session &s, dl_progress *progress) {
     uint32_t *words = P.get<uint32_t>("words", total_words);
     uint32_t *entry_pair = P.get<uint32_t>("entry_pair", kept);
     unsigned long long *entry_dst = P.get<unsigned long long>("entry_dst", kept);
+    unsigned long long *entry_bdst = P.get<unsigned long long>("entry_bdst", kept);
     if (T) {
-        k_serialize<<<grid_for(T), kBlock, 0, st>>>(sc, tri_off, pair_light, keep, tri_crop, stride, ld_scan, pl_scan,
-                                                    mesh_base, entry_off, words, entry_pair, entry_dst);
+        k_serialize<<<grid_for(T), kBlock, 0, st>>>(sc, tri_off, pair_light, keep, pair_bounce, tri_crop, stride, ld_scan,
+                                                    pl_scan, mesh_base, entry_off, words, entry_pair, entry_dst,
+                                                    entry_bdst);
         LAUNCHED("k_serialize");
         ++s.launches;
     }
@@ -1234,6 +1682,12 @@ dl_status run(dl_session &s, dl_progress *progress) {
                                                                tri_crop, region_rect, region_off, region_pool, words);
         LAUNCHED("k_crop");
         ++s.launches;
+        if (bmap) {
+            k_pack_bounce<<<grid_for(kept), kBlock, 0, st>>>(sc, kept, entry_pair, entry_bdst, pair_tri, pair_light,
+                                                             tri_crop, region_rect, woff, bmap, words);
+            LAUNCHED("k_pack_bounce");
+            ++s.launches;
+        }
     }
     CK(cudaEventRecord(e1, st));
     s.mesh_words.resize(M + 1);
@@ -1249,7 +1703,6 @@ dl_status run(dl_session &s, dl_progress *progress) {
     s.report.shadow_rays = s.counters.rays;
     s.report.burial_rays = s.counters.burial_rays;
     s.report.bounce_rays = s.counters.bounce_rays;
-    s.report.photon_rays = s.counters.photon_rays;
     s.report.node_visits = s.counters.node_visits;
     s.report.tri_tests = s.counters.tri_tests;
     s.report.kernel_launches = s.launches;

@@ -274,9 +274,30 @@ dl_status prepare_scene(const dl_bake_input &in, const dl_bake_options &o, HostS
         s.lights.push_back(d);
         s.bounce_in_scene |= bounce;
     }
-    if (s.bounce_in_scene) {
-        err = "one-bounce lighting is not baked by this build of the library";
-        return DL_UNSUPPORTED;
+    // photon cubes for local bounce lights, in slot order (bounce.rs:126-151)
+    for (uint32_t i = 0; i < s.lights.size(); ++i) {
+        DevLight &d = s.lights[i];
+        d.cube = 0xFFFFFFFFu;
+        if ((d.flags & kLightBounce) && d.shape != DL_SHAPE_SUN) {
+            d.cube = (uint32_t)s.cube_lights.size();
+            s.cube_lights.push_back(i);
+        }
+    }
+    // gaussian_weights(7, 5.0) (bounce_map.rs:140-151): f32 arithmetic, exp rounded once
+    {
+        const float sigma2 = 5.0f * 5.0f;
+        float sum = 0.0f;
+        for (int i = -3; i <= 3; ++i) {
+            float w = (1.0f / sqrtf(2.0f * kPiF * sigma2)) * (float)std::exp((double)(-(float)(i * i) / (2.0f * sigma2)));
+            s.blur_weights[i + 3] = w;
+            sum += w;
+        }
+        float total = 0.0f;
+        for (int k = 0; k < 7; ++k) {
+            s.blur_weights[k] = s.blur_weights[k] / sum;
+            total += s.blur_weights[k];
+        }
+        s.blur_weight_sum = total;
     }
 
     // PreparedMesh resolution (mesh_builder.rs:21-51, geometry.rs:66-70) and the occluders

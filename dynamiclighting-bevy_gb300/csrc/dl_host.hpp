@@ -33,7 +33,8 @@ struct DevLight {
     uint32_t bounce_bits;  // 0: no bounce
     uint64_t id;
     f3 bounds_lo, bounds_hi;  // light_bounds (light_bvh.rs:77-81), local lights only
-    uint32_t pad[2];
+    uint32_t cube;            // photon cube index of a local bounce light, else ~0
+    uint32_t pad;
 };
 enum : uint32_t {
     kLightDistant = 1,
@@ -62,6 +63,9 @@ struct HostScene {
     std::vector<dl_light_bvh_node> light_bvh;
     bool bounce_in_scene = false;
     std::vector<uint32_t> resolution;  // per mesh
+    std::vector<uint32_t> cube_lights;  // slot of each photon cube's light (bounce.rs:126-151)
+    float blur_weights[7];              // gaussian_weights(7, 5) (bounce_map.rs:140-151)
+    float blur_weight_sum;
     uint64_t triangles = 0;
     // occluders in the reference's order (sorted mesh order, triangle order, non-degenerate)
     std::vector<uint32_t> occ_mesh, occ_tri;

@@ -368,3 +368,218 @@ __device__ __forceinline__ bool is_buried(const DevScene &sc, f3 normal, f3 orig
 }
 
 }  // namespace dl
+
+namespace dl {
+
+// ---- one bounce (src/bake/bounce.rs, sun_bounce.rs, shared/cube.rs) --------------------------
+
+// A photon (bounce.rs:29-39): distance, normal as i8 x 3 and albedo as u8 x 3.
+struct Photon {
+    float distance;
+    uint32_t normal;  // bytes x, y, z (two's complement)
+    uint32_t albedo;  // bytes r, g, b
+};
+
+// face_uv_to_direction / texel_direction (cube.rs:57-79)
+__device__ __forceinline__ f3 cube_texel_direction(uint32_t face, uint32_t x, uint32_t y, uint32_t res) {
+    float size = (float)res;
+    float sc = ((float)x + 0.5f) / size * 2.0f - 1.0f, tc = ((float)y + 0.5f) / size * 2.0f - 1.0f;
+    f3 d;
+    switch (face) {
+        case 0: d = f3{1.0f, -tc, -sc}; break;
+        case 1: d = f3{-1.0f, -tc, sc}; break;
+        case 2: d = f3{sc, 1.0f, tc}; break;
+        case 3: d = f3{sc, -1.0f, -tc}; break;
+        case 4: d = f3{sc, -tc, 1.0f}; break;
+        default: d = f3{-sc, -tc, -1.0f}; break;
+    }
+    return normalize(d);
+}
+// direction_to_face_uv + direction_to_texel (cube.rs:29-53, 94-105): the flat texel index.
+__device__ __forceinline__ uint32_t cube_texel_index(f3 d, uint32_t res) {
+    f3 a{fabsf(d.x), fabsf(d.y), fabsf(d.z)};
+    uint32_t face;
+    float sc, tc, ma;
+    if (a.x > a.y && a.x > a.z) {
+        if (d.x > 0.0f) { face = 0; sc = -d.z; tc = -d.y; }
+        else { face = 1; sc = d.z; tc = -d.y; }
+        ma = a.x;
+    } else if (a.y > a.z) {
+        if (d.y > 0.0f) { face = 2; sc = d.x; tc = d.z; }
+        else { face = 3; sc = d.x; tc = -d.z; }
+        ma = a.y;
+    } else if (d.z > 0.0f) {
+        face = 4; sc = d.x; tc = -d.y; ma = a.z;
+    } else {
+        face = 5; sc = -d.x; tc = -d.y; ma = a.z;
+    }
+    float u = 0.5f, v = 0.5f;
+    if (ma != 0.0f) {
+        u = (sc / ma) * 0.5f + 0.5f;
+        v = (tc / ma) * 0.5f + 0.5f;
+    }
+    float max = (float)(res - 1);
+    uint32_t x = f2u(clampf(floorf(u * (float)res), 0.0f, max));
+    uint32_t y = f2u(clampf(floorf(v * (float)res), 0.0f, max));
+    return face * res * res + y * res + x;
+}
+
+// Occluder::face_normal / surface_normal / albedo (occluder.rs:117-144) at a closest hit.
+__device__ __forceinline__ f3 hit_face_normal(const DevScene &sc, const Hit &h) {
+    uint32_t leaf = sc.occ_leaf[h.occluder];
+    float4 e1 = ldg4(sc.tri_e1 + leaf), e2 = ldg4(sc.tri_e2 + leaf);
+    return normalize_or_zero(cross(f3{e1.x, e1.y, e1.z}, f3{e2.x, e2.y, e2.z}));
+}
+__device__ __forceinline__ f3 hit_surface_normal(const DevScene &sc, const Hit &h, f3 face) {
+    uint32_t m = sc.occ_mesh[h.occluder];
+    if (!(sc.mesh_flags[m] & kMeshNormals)) return face;
+    const uint32_t *c = sc.indices + sc.mesh_index_base[m] + (size_t)sc.occ_tri[h.occluder] * 3;
+    uint32_t vb = sc.mesh_vertex_base[m];
+    float wx = 1.0f - h.u - h.v;
+    f3 n{0.0f, 0.0f, 0.0f};
+    for (int k = 0; k < 3; ++k) {
+        size_t vi = (size_t)vb + c[k];
+        f3 nv{sc.normals[vi * 3], sc.normals[vi * 3 + 1], sc.normals[vi * 3 + 2]};
+        float w = k == 0 ? wx : k == 1 ? h.u : h.v;
+        n = k == 0 ? scale(nv, w) : add(n, scale(nv, w));
+    }
+    bool ok;
+    f3 t = try_normalize(n, ok);
+    return ok ? t : face;
+}
+__device__ __forceinline__ f3 hit_albedo(const DevScene &sc, const Hit &h) {
+    const float *a = sc.mesh_albedo + (size_t)sc.occ_mesh[h.occluder] * 3;
+    return f3{a[0], a[1], a[2]};
+}
+
+// photon (bounce.rs:88-115)
+__device__ __forceinline__ Photon make_photon(const DevScene &sc, const DevLight &l, f3 dir, int *stack, int stride) {
+    Hit h;
+    if (!traverse<false>(sc, l.position, dir, l.radius, (l.flags & kLightAlpha) != 0, stack, stride, h))
+        return Photon{l.radius, 0u, 0u};
+    f3 face = hit_face_normal(sc, h);
+    f3 normal = hit_surface_normal(sc, h, face);
+    f3 point = add(l.position, scale(dir, h.t));
+    float bias = fmaxf(h.t * 0.001f, 0.001f);
+    f3 nudged = add(sub(point, scale(dir, bias)), scale(normal, bias));
+    bool lit_side = dot(face, dir) < 0.0f;
+    Photon p;
+    p.distance = length(sub(nudged, l.position));
+    p.normal = 0;
+    if (lit_side) {
+        uint32_t nx = (uint32_t)(f2i8(roundf(normal.x * 127.0f)) & 0xFF);
+        uint32_t ny = (uint32_t)(f2i8(roundf(normal.y * 127.0f)) & 0xFF);
+        uint32_t nz = (uint32_t)(f2i8(roundf(normal.z * 127.0f)) & 0xFF);
+        p.normal = nx | (ny << 8) | (nz << 16);
+    }
+    f3 a = hit_albedo(sc, h);
+    p.albedo = f2u8(roundf(clampf(a.x, 0.0f, 1.0f) * 255.0f)) | (f2u8(roundf(clampf(a.y, 0.0f, 1.0f) * 255.0f)) << 8) |
+               (f2u8(roundf(clampf(a.z, 0.0f, 1.0f) * 255.0f)) << 16);
+    return p;
+}
+
+// Spherical interpolation with linearly interpolated length (glam Vec3::slerp's structure,
+// restated from the standard formula: sin-weighted blend over the angle acos(a.b / |a||b|); a
+// plain lerp when nearly parallel, a half turn about an orthogonal axis when nearly opposite).
+__device__ __forceinline__ float lerpf(float a, float b, float s) { return a + (b - a) * s; }
+__device__ __forceinline__ f3 slerp3(f3 a, f3 b, float s) {
+    float la = length(a), lb = length(b);
+    float d = dot(a, b) / (la * lb);
+    if (fabsf(d) < 1.0f - 3e-7f) {
+        float theta = acos_f(d);
+        float sin_theta = sin_f(theta);
+        float t1 = sin_f(theta * (1.0f - s));
+        float t2 = sin_f(theta * s);
+        float rl = lerpf(la, lb, s);
+        return scale(add(scale(scale(a, rl / la), t1), scale(scale(b, rl / lb), t2)), 1.0f / sin_theta);
+    }
+    if (d < 0.0f) {
+        f3 axis = normalize(fabsf(a.x) > fabsf(a.y) ? f3{-a.z, 0.0f, a.x} : f3{0.0f, a.z, -a.y});
+        float sp, cp;
+        sincos_f(kPiF * s, sp, cp);
+        f3 turned = add(scale(a, cp), scale(cross(axis, a), sp));
+        return scale(turned, lerpf(la, lb, s) / la);
+    }
+    return add(scale(a, 1.0f - s), scale(b, s));
+}
+
+__device__ __forceinline__ f3 reflected(const DevScene &sc, f3 albedo) {
+    return sc.colored_bounce ? albedo : f3{1.0f, 1.0f, 1.0f};
+}
+
+// gather_triangle's per-texel body (bounce.rs:252-289). Returns false when the texel is out of
+// the light's reach (it then gathers nothing and sets no map texel).
+template <class TR>
+__device__ __forceinline__ bool gather_local(const DevScene &sc, const DevLight &l, const Photon *cube, uint32_t res,
+                                             uint64_t mesh_id, uint32_t x, uint32_t y, f3 pos, f3 normal,
+                                             const TR &tr, f3 &value, uint32_t &rays) {
+    f3 to_texel = sub(pos, l.position);
+    if (length_sq(to_texel) > l.radius * l.radius) return false;
+    f3 direction = normalize_or(to_texel, f3{0.0f, 1.0f, 0.0f});
+    Pcg rng = stream5(sc.seed, mesh_id, l.id, x, y);
+    uint32_t samples = l.bounce_samples;
+    float step = 0.9f / (float)(samples - 1);
+    f3 sum{0.0f, 0.0f, 0.0f};
+    for (uint32_t i = 0; i < samples; ++i) {
+        float spread_s = 0.1f + (float)i * step;
+        f3 random = on_unit_sphere(rng);
+        f3 sample = normalize_or(slerp3(direction, random, spread_s), direction);
+        Photon ph = cube[cube_texel_index(sample, res)];
+        f3 pn{(float)(int8_t)(ph.normal & 0xFF) / 127.0f, (float)(int8_t)((ph.normal >> 8) & 0xFF) / 127.0f,
+              (float)(int8_t)((ph.normal >> 16) & 0xFF) / 127.0f};
+        pn = normalize_or_zero(pn);
+        f3 photon = add(l.position, scale(sample, ph.distance));
+        f3 albedo{(float)(ph.albedo & 0xFF) / 255.0f, (float)((ph.albedo >> 8) & 0xFF) / 255.0f,
+                  (float)((ph.albedo >> 16) & 0xFF) / 255.0f};
+        f3 to_photon = sub(photon, tr.origin);
+        float distance = length(to_photon);
+        if (is_zero(pn) || distance <= 0.0f) continue;
+        f3 d = divs(to_photon, distance);
+        ++rays;
+        if (!tr(d, distance)) {
+            float weight = fmaxf(dot(normal, d), 0.0f) * fmaxf(dot(pn, neg(d)), 0.0f);
+            sum = add(sum, scale(reflected(sc, albedo), weight));
+        }
+    }
+    value = divs(scale(sum, l.bounce_intensity), (float)samples);
+    return true;
+}
+
+// gather_sun's per-texel body (sun_bounce.rs:333-370).
+__device__ __forceinline__ void gather_sun(const DevScene &sc, const DevLight &l, uint64_t mesh_id, uint32_t x,
+                                           uint32_t y, f3 origin, f3 normal, int *stack, int stride, f3 &value,
+                                           uint32_t &rays) {
+    bool alpha = (l.flags & kLightAlpha) != 0;
+    Pcg rng = stream5(sc.seed, mesh_id, l.id, x, y);
+    f2 off;
+    off.x = rng.next_f32();
+    off.y = rng.next_f32();
+    uint32_t samples = l.bounce_samples;
+    f3 sum{0.0f, 0.0f, 0.0f};
+    for (uint32_t i = 0; i < samples; ++i) {
+        f3 direction = cosine_direction(normal, spread(i, off, true));
+        ++rays;
+        Hit h;
+        if (!traverse<false>(sc, origin, direction, INFINITY, alpha, stack, stride, h)) continue;
+        f3 face = hit_face_normal(sc, h);
+        if (dot(face, direction) >= 0.0f) continue;
+        float lit = dot(hit_surface_normal(sc, h, face), l.toward);
+        if (lit <= 0.0f || dot(face, l.toward) <= 0.0f) continue;
+        f3 point = add(add(origin, scale(direction, h.t)), scale(face, kRayOffset));
+        ++rays;
+        if (!occluded(sc, point, l.toward, INFINITY, alpha, stack, stride))
+            sum = add(sum, scale(reflected(sc, hit_albedo(sc, h)), lit));
+    }
+    value = divs(scale(sum, l.bounce_intensity), (float)samples);
+}
+
+// quantize (bounce_pack.rs:74-86)
+__device__ __forceinline__ uint32_t quantize_bounce(float value, uint32_t bits, Pcg &rng) {
+    float max = (float)((1u << bits) - 1);
+    float amplitude = bits == 8 ? 0.0f : bits == 6 ? 0.004f : bits == 5 ? 0.008f : 0.02f;
+    float color = isnan(value) ? 0.0f : clampf(value, 0.0f, 1.0f);
+    if (amplitude > 0.0f && color > 0.001f) color = fminf(color + rng.next_f32() * amplitude, 1.0f);
+    return f2u(sqrtf(color) * max);
+}
+
+}  // namespace dl

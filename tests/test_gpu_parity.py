@@ -68,14 +68,40 @@ def test_soft_rooms_batched_and_plain_agree_with_the_oracle():
     assert_same(plain, want)
 
 
-def test_outdoor_slice_with_sun_and_sky():
+def test_outdoor_slice_with_sun_sky_and_colored_sun_bounce():
     inp, opts = scenes.outdoor(grid=65, chunks=2, boxes=40, point_lights=6, sky_samples=32,
                                bounce_samples=8)
-    for l in inp.lights:
-        l.illumination = dl.DIRECT
     want, _, _ = oracle.bake(inp, opts)
     got = dl.bake(inp, opts)
+    assert got.settings["bounce"] and got.settings["colored_bounce"]
     assert_same(got, want)
+
+
+@pytest.mark.parametrize("compression", [8, 6, 4])
+def test_local_light_bounce_matches_the_oracle(compression):
+    # photon cubes, slerp gathers, last-triangle-wins maps, dilate/blur, dithered packing
+    inp, opts = scenes.room_grid(rooms=2, lights=6, boxes_per_room=6, samples=16)
+    opts.photon_cube_resolution = 64
+    opts.bounce_compression = compression
+    want, _, _ = oracle.bake(inp, opts)
+    report = dl._abi.DlBakeReport()
+    got = dl.bake(inp, opts, report=report)
+    assert want.stats["bounce_rays"] > 0
+    assert_same(got, want)
+    assert report.photon_rays == 6 * 64 * 64 * 6
+
+
+def test_colored_bounce_with_mixed_lights():
+    inp, opts = fx.determinism_room()
+    for l in inp.lights:
+        if l.shape.kind != dl.SKY:
+            l.illumination = dl.SINGLE_BOUNCE
+            l.bounce = dl.BakeBounce(samples=12, intensity=1.5, compression=5 if l.id % 20 == 0 else None)
+    opts.colored_bounce = True
+    opts.photon_cube_resolution = 48
+    want, _, _ = oracle.bake(inp, opts)
+    for form in ("batched", "plain"):
+        assert_same(dl.bake(inp, opts, form=form), want)
 
 
 def test_alpha_tested_shadows():
