@@ -360,6 +360,9 @@ def load_library(path: str = LIBRARY_PATH):
     lib.dl_encode_payload.argtypes = [P(DlBakedScene), P(P(C.c_uint8)), P(C.c_uint64),
                                       P(C.c_uint32)]
     lib.dl_free.argtypes = [C.c_void_p]
+    lib.dl_filter_bounce_window_noalloc.restype = C.c_int
+    lib.dl_filter_bounce_window_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+                                                    C.c_uint32, C.c_uint32, C.c_void_p]
     _LIB = lib
     return lib
 

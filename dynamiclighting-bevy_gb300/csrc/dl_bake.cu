@@ -1972,3 +1972,154 @@ dl_status dl_encode_payload(const dl_baked_scene *scene, uint8_t **bytes, uint64
 void dl_free(void *p) { std::free(p); }
 
 }  // extern "C"
+
+// ================================ non-allocating bounce filter ============================
+//
+// dl_filter_bounce_window_noalloc: the bounce map filter of the bake (dilate, then the 7-tap
+// separable blur; the body of k_bounce_filter) on one window held in caller-owned device
+// buffers, for callers that cannot allocate device memory — an engine applying the filter from
+// inside its own fixed memory budget, or from code that must not call cudaMalloc (while a
+// stream is being captured, or on a frame thread). The blur's intermediate lives in the
+// fixed array below, which every device that loads the library holds until the process exits.
+
+namespace dl {
+
+constexpr uint32_t kNoallocMaxTexels = DL_NOALLOC_MAX_TEXELS;
+static __device__ __align__(256) float g_noalloc_scratch[3 * (size_t)kNoallocMaxTexels];
+
+namespace {
+
+constexpr int kNoallocDevices = 64;
+std::mutex g_noalloc_mutex;
+float *g_noalloc_ptr[kNoallocDevices] = {};
+
+// Dilation (bounce_map.rs:67-87): the first positive texel among itself and its 8 neighbours in
+// a fixed order; outside the window reads 0.
+__global__ void k_noalloc_dilate(const float *in, float *out, uint32_t w, uint32_t h) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w * h) return;
+    int x = (int)(i % w), y = (int)(i / w);
+    const int order[9][2] = {{0, 0}, {-1, -1}, {0, -1}, {1, -1}, {-1, 0}, {1, 0}, {-1, 1}, {0, 1}, {1, 1}};
+    float r = 0.0f, g = 0.0f, b = 0.0f;
+    for (int k = 0; k < 9; ++k) {
+        int xx = x + order[k][0], yy = y + order[k][1];
+        if (xx < 0 || yy < 0 || xx >= (int)w || yy >= (int)h) continue;
+        const float *v = in + ((size_t)yy * w + xx) * 3;
+        if (fmaxf(fmaxf(v[0], v[1]), v[2]) > 0.0f) {
+            r = v[0];
+            g = v[1];
+            b = v[2];
+            break;
+        }
+    }
+    out[(size_t)i * 3] = r;
+    out[(size_t)i * 3 + 1] = g;
+    out[(size_t)i * 3 + 2] = b;
+}
+
+struct BlurWeights {
+    float w[7];
+    float sum;
+};
+
+// One blur pass (bounce_map.rs:92-112): sample coordinates clamped to the map, reads outside
+// the window are 0, sum in tap order, divided by the weights' sum.
+__global__ void k_noalloc_blur(const float *src, float *dst, uint32_t w, uint32_t h, uint32_t x0, uint32_t y0,
+                               uint32_t map_size, int vertical, BlurWeights bw) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w * h) return;
+    int64_t x = x0 + (int64_t)(i % w), y = y0 + (int64_t)(i / w);
+    int64_t last = (int64_t)map_size - 1;
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+    for (int k = -3; k <= 3; ++k) {
+        int64_t qx = vertical ? x : min(max(x + k, (int64_t)0), last);
+        int64_t qy = vertical ? min(max(y + k, (int64_t)0), last) : y;
+        float r = 0.0f, g = 0.0f, b = 0.0f;
+        if (qx >= (int64_t)x0 && qy >= (int64_t)y0 && qx < (int64_t)x0 + w && qy < (int64_t)y0 + h) {
+            const float *v = src + ((size_t)(qy - y0) * w + (size_t)(qx - x0)) * 3;
+            r = v[0];
+            g = v[1];
+            b = v[2];
+        }
+        sx = sx + r * bw.w[k + 3];
+        sy = sy + g * bw.w[k + 3];
+        sz = sz + b * bw.w[k + 3];
+    }
+    dst[(size_t)i * 3] = sx / bw.sum;
+    dst[(size_t)i * 3 + 1] = sy / bw.sum;
+    dst[(size_t)i * 3 + 2] = sz / bw.sum;
+}
+
+// gaussian_weights(7, 5.0) (bounce_map.rs:140-151) in f32, exp rounded once from binary64.
+BlurWeights blur_weights() {
+    BlurWeights bw{};
+    const float sigma2 = 5.0f * 5.0f;
+    float sum = 0.0f;
+    for (int i = -3; i <= 3; ++i) {
+        float w = (1.0f / sqrtf(2.0f * kPiF * sigma2)) * (float)std::exp((double)(-(float)(i * i) / (2.0f * sigma2)));
+        bw.w[i + 3] = w;
+        sum += w;
+    }
+    for (int k = 0; k < 7; ++k) {
+        bw.w[k] = bw.w[k] / sum;
+        bw.sum += bw.w[k];
+    }
+    return bw;
+}
+
+}  // namespace
+}  // namespace dl
+
+extern "C" dl_status dl_filter_bounce_window_noalloc(const float *in_rgb, float *out_rgb, uint32_t width,
+                                                     uint32_t height, uint32_t x0, uint32_t y0, uint32_t map_size,
+                                                     void *stream) {
+    using namespace dl;
+    if (!in_rgb || !out_rgb || in_rgb == out_rgb) {
+        g_error = "the input and output windows must be distinct device buffers";
+        return DL_INVALID_ARGUMENT;
+    }
+    uint64_t n = (uint64_t)width * height;
+    if (width == 0 || height == 0 || n > kNoallocMaxTexels) {
+        g_error = "window of " + std::to_string(width) + " x " + std::to_string(height) +
+                  " texels: the non-allocating filter takes 1 to " + std::to_string(kNoallocMaxTexels) + " texels";
+        return DL_INVALID_ARGUMENT;
+    }
+    if ((uint64_t)x0 + width > map_size || (uint64_t)y0 + height > map_size) {
+        g_error = "the window does not lie inside the map";
+        return DL_INVALID_ARGUMENT;
+    }
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess || device < 0 || device >= kNoallocDevices) {
+        g_error = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
+        return DL_CUDA_ERROR;
+    }
+    float *scratch = nullptr;
+    {
+        // set-up, once per device, with that device current: the scratch array's device address
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_ptr[device]) {
+            e = cudaGetSymbolAddress((void **)&g_noalloc_ptr[device], g_noalloc_scratch);
+            if (e != cudaSuccess) {
+                g_noalloc_ptr[device] = nullptr;
+                g_error = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+                return DL_CUDA_ERROR;
+            }
+        }
+        scratch = g_noalloc_ptr[device];
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    BlurWeights bw = blur_weights();
+    unsigned blocks = (unsigned)((n + 255) / 256);
+    // dilate into the output, blur across into the scratch, blur down into the output; every
+    // scratch texel is written before it is read, so nothing needs clearing between calls
+    k_noalloc_dilate<<<blocks, 256, 0, st>>>(in_rgb, out_rgb, width, height);
+    k_noalloc_blur<<<blocks, 256, 0, st>>>(out_rgb, scratch, width, height, x0, y0, map_size, 0, bw);
+    k_noalloc_blur<<<blocks, 256, 0, st>>>(scratch, out_rgb, width, height, x0, y0, map_size, 1, bw);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        g_error = std::string("bounce filter launch: ") + cudaGetErrorString(e);
+        return DL_CUDA_ERROR;
+    }
+    return DL_OK;
+}

@@ -291,6 +291,27 @@ dl_status dl_encode_payload(const dl_baked_scene *scene, uint8_t **bytes, uint64
                             uint32_t *crc32);
 void dl_free(void *pointer);
 
+/* ---- Non-allocating bounce filter. No counterpart in the reference: its BounceMap filter
+ * (src/bake/bounce_map.rs:67-112) runs only inside bake(). For callers that cannot allocate
+ * device memory (a fixed engine memory budget, code running while a stream is captured, a frame
+ * thread), this applies the same dilation and 7-tap separable blur to one window of a bounce map
+ * held in caller-owned device buffers and allocates nothing.
+ *
+ * in_rgb / out_rgb: distinct device buffers of width * height RGB float triples, row-major; the
+ * window covers map texels [x0, x0 + width) x [y0, y0 + height) of a map_size^2 map (the blur
+ * clamps to the map and reads 0 outside the window, as the bake does). At most
+ * DL_NOALLOC_MAX_TEXELS texels, else DL_INVALID_ARGUMENT. Runs on the calling thread's current
+ * device, enqueued on `stream` (a cudaStream_t, NULL for the legacy default stream).
+ *
+ * The blur's intermediate lives in one fixed device array of DL_NOALLOC_MAX_TEXELS * 12 bytes
+ * (3 MiB) that every device loading the library holds until the process exits. The first call on
+ * a device looks up that array's address (cudaGetSymbolAddress); make it before any stream
+ * capture. All calls share the array: calls whose work overlaps on the GPU (concurrent streams,
+ * threads) race on it, so serialize them. */
+#define DL_NOALLOC_MAX_TEXELS (512u * 512u)
+dl_status dl_filter_bounce_window_noalloc(const float *in_rgb, float *out_rgb, uint32_t width, uint32_t height,
+                                          uint32_t x0, uint32_t y0, uint32_t map_size, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -442,6 +442,18 @@ static uint64_t gather_sun(const Scene &sc, const std::vector<SurfaceTexel> &tex
     return rays;
 }
 
+// A test hook: the bounce map of one (mesh id, light slot) before and after its filters.
+struct BounceCapture {
+    bool on = false;
+    uint64_t mesh_id = 0;
+    uint32_t slot = 0;
+    bool taken = false;
+    Rect rect{};
+    uint32_t size = 0;
+    std::vector<V3> pre, post;
+};
+static BounceCapture g_capture;
+
 // bake_mesh_bounce (bounce.rs:155-217): result[t][k] = padded bounce grid or empty.
 static uint64_t mesh_bounce(const Scene &sc, const Prepared &p, const std::vector<Setup> &setups,
                             const MeshTexels &mt, std::vector<std::vector<std::vector<V3>>> &result,
@@ -483,8 +495,16 @@ static uint64_t mesh_bounce(const Scene &sc, const Prepared &p, const std::vecto
             rays += counts[i];
             for (auto &g : gathered[i]) map.set(g.x, g.y, g.value);
         }
+        bool capture = g_capture.on && g_capture.mesh_id == p.mesh->id && g_capture.slot == slot;
+        if (capture) {
+            g_capture.taken = true;
+            g_capture.rect = map.rect;
+            g_capture.size = map.size;
+            g_capture.pre = map.values;
+        }
         map.dilate();
         map.blur();
+        if (capture) g_capture.post = map.values;
         for (auto &r : receivers) has[r.first][r.second] = map.crop(setups[r.first].crop, result[r.first][r.second]);
     }
     return rays;
@@ -871,6 +891,29 @@ int oracle_bake(const dl_bake_input *in, const dl_bake_options *o, const dl_prog
     return DL_OK;
 }
 void oracle_free(dl_baked_scene *s) { delete reinterpret_cast<Result *>(s); }
+
+// Arms the bounce-map capture of (mesh id, light slot) for the next oracle_bake.
+void oracle_capture_bounce(uint64_t mesh_id, uint32_t slot) {
+    g_capture = BounceCapture{};
+    g_capture.on = true;
+    g_capture.mesh_id = mesh_id;
+    g_capture.slot = slot;
+}
+// The captured window (rect min_x, min_y, max_x, max_y; map size) and its texels before and after
+// the filters, RGB floats; returns the texel count (0 when nothing was captured).
+uint32_t oracle_captured_bounce(uint32_t rect[4], uint32_t *size, float *pre, float *post, uint32_t cap) {
+    if (!g_capture.taken) return 0;
+    rect[0] = g_capture.rect.min_x; rect[1] = g_capture.rect.min_y;
+    rect[2] = g_capture.rect.max_x; rect[3] = g_capture.rect.max_y;
+    *size = g_capture.size;
+    uint32_t n = (uint32_t)g_capture.pre.size();
+    for (uint32_t i = 0; i < n && i < cap; ++i) {
+        pre[i * 3] = g_capture.pre[i].x; pre[i * 3 + 1] = g_capture.pre[i].y; pre[i * 3 + 2] = g_capture.pre[i].z;
+        post[i * 3] = g_capture.post[i].x; post[i * 3 + 1] = g_capture.post[i].y; post[i * 3 + 2] = g_capture.post[i].z;
+    }
+    g_capture.on = false;
+    return n;
+}
 
 // ---- known-answer hooks (one per reference unit test family) ----------------------------------
 uint32_t oracle_lightmap_size(float area, float density, uint32_t max_size) {
