@@ -31,20 +31,28 @@ PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 
 WORKLOADS = {
-    # name: (generator kwargs, description)
+    # name: (generator, description)
+    "outdoor": (lambda: scenes.outdoor(),
+                "512x512 fBm heightfield (522k tris, 8x8 chunks) + 2000 boxes/planks = 546k tris; 0.53 deg "
+                "sun, 4-bit, 5 probes + 16..32 disk samples; colored sun bounce, 128 samples; sky, 256 samples; "
+                "32 point lights; 4 texels/m"),
+    "room_grid": (lambda: scenes.room_grid(),
+                  "6x6 rooms 8x3.5x8 m with doorways, 20 boxes/ramps each (44.5k tris); 64 point lights, "
+                  "radius U[4,12]; 1-bit shadows + one bounce, 64 gather samples, 512^2 photon cubes; 16 texels/m"),
     "soft_rooms": (lambda: scenes.soft_rooms(),
-                   "6x6 rooms re-meshed with log-normal triangles, 128 lights (64 point, 32 rectangle, "
-                   "32 tube), 4-bit soft shadows from 16 samples, 16 texels/m"),
+                   "6x6 rooms re-meshed with log-normal triangles (106k tris), 128 lights (64 point, 32 rectangle, "
+                   "32 tube), 4-bit soft shadows from 5/3 probes + 16 samples, 16 texels/m"),
     "small_room": (lambda: scenes.small_room(),
-                   "10x4x10 m room + 5 cubes, 4 point lights, 1-bit, 8 texels/m"),
-    "room_grid_direct": (lambda: scenes.room_grid(bounce=False),
-                         "6x6 rooms with doorways and 20 boxes/ramps each, 64 point lights, direct only"),
+                   "10x4x10 m room + 5 cubes (72 tris), 4 point lights, 1-bit, 8 texels/m"),
 }
-# The CPU baseline bakes a smaller instance of the same generator (rays/s is intensive).
+# The CPU baseline bakes a smaller instance of the same generator with the same light kinds and
+# sample counts (rays/s is intensive).
 CPU_SAMPLES = {
+    "outdoor": (lambda: scenes.outdoor(grid=97, chunks=2, boxes=72, point_lights=2),
+                "96x96 m of the same terrain generator with 72 boxes, 2 point lights, the same sun/sky/bounce"),
+    "room_grid": (lambda: scenes.room_grid(rooms=2, lights=7), "2x2 rooms, 7 lights, same samples"),
     "soft_rooms": (lambda: scenes.soft_rooms(rooms=2, lights=14, boxes_per_room=20), "2x2 rooms, 14 lights"),
     "small_room": (lambda: scenes.small_room(), "the full workload"),
-    "room_grid_direct": (lambda: scenes.room_grid(rooms=2, lights=8, bounce=False), "2x2 rooms, 8 lights"),
 }
 
 

@@ -1100,12 +1100,15 @@ struct dl_session {
     Counters counters{};
     uint64_t texels = 0;
     // batched-form graph over the visibility stage, rebuilt when the queue changes
+    cudaEvent_t marks[8] = {};  // stage boundaries of the last run
     cudaGraphExec_t graph = nullptr;
     uint64_t graph_generation = ~0ull;
     unsigned long long graph_items = 0;
     unsigned graph_blocks = 0;
     ~dl_session() {
         if (graph) cudaGraphExecDestroy(graph);
+        for (auto &e : marks)
+            if (e) cudaEventDestroy(e);
         for (void *p : owned) cudaFree(p);
         if (stream) cudaStreamDestroy(stream);
         if (side) cudaStreamDestroy(side);
@@ -1283,6 +1286,7 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     sc.colored_bounce = o->colored_bounce;
     s->ctr = dev_alloc<Counters>(s->owned, 1, bytes);
     s->cancel_dev = dev_alloc<uint32_t>(s->owned, 1, bytes);
+    for (auto &e : s->marks) CK(cudaEventCreate(&e));
     s->report.bvh_nodes = h.nodes.size();
     s->report.occluders = N;
     out = s.release();
@@ -1339,6 +1343,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
         return DL_OK;
     }
 
+    CK(cudaEventRecord(s.marks[0], st));
     // ---- setup + association
     float4 *tri_face = P.get<float4>("tri_face", T);
     uint4 *tri_crop = P.get<uint4>("tri_crop", T);
@@ -1378,6 +1383,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
     uint32_t *region_pool = P.get<uint32_t>("region_pool", region_total);
     CK(cudaMemsetAsync(region_pool, 0, region_total * 4ull, st));
 
+    CK(cudaEventRecord(s.marks[1], st));
     // ---- texels
     uint64_t *grid_off = P.get<uint64_t>("grid_off", M + 1);
     CK(cudaMemcpyAsync(grid_off, s.grid_off.data(), (M + 1) * 8ull, cudaMemcpyHostToDevice, st));
@@ -1415,6 +1421,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
         LAUNCHED("k_texels");
         ++s.launches;
     }
+    CK(cudaEventRecord(s.marks[2], st));
     if (texels_all) {
         k_burial<<<grid_for(texels_all), kBlock, 0, st>>>(sc, texels_all, tex_xy, tex_pos, tex_tri, tri_face, buried,
                                                           s.ctr);
@@ -1444,6 +1451,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
     s.texels = texels;
     if (check_cancel()) return DL_CANCELLED;
 
+    CK(cudaEventRecord(s.marks[3], st));
     // ---- visibility
     TraceArgs ta{};
     ta.pair_tri = pair_tri;
@@ -1533,6 +1541,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
     wait(s, progress);
     if (check_cancel()) return DL_CANCELLED;
 
+    CK(cudaEventRecord(s.marks[4], st));
     // ---- one bounce: photon cubes, gathers, bounce maps (bounce.rs:48-217)
     const HostScene &hs = s.host;
     uint8_t *pair_bounce = P.get<uint8_t>("pair_bounce", pairs);
@@ -1624,6 +1633,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
         s.launches += 3;
     }
 
+    CK(cudaEventRecord(s.marks[5], st));
     // ---- optimize, seams
     uint8_t *keep = P.get<uint8_t>("keep", pairs);
     uint32_t *kept_cnt = P.get<uint32_t>("kept_cnt", T + 1);
@@ -1647,6 +1657,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
     scan_u32(s, kept_cnt, entry_off, T + 1);
     const uint32_t kept = read_back(s, entry_off + T);
 
+    CK(cudaEventRecord(s.marks[6], st));
     // ---- serialize
     const uint32_t stride = s.host.bounce_in_scene ? 3 : 2;
     unsigned long long *ld_words = P.get<unsigned long long>("ld_words", T + 1);
@@ -1690,6 +1701,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
         }
     }
     CK(cudaEventRecord(e1, st));
+    CK(cudaEventRecord(s.marks[7], st));
     s.mesh_words.resize(M + 1);
     CK(cudaMemcpyAsync(s.mesh_words.data(), mesh_words, (M + 1) * 8ull, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&s.counters, s.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
@@ -1699,6 +1711,11 @@ dl_status run(dl_session &s, dl_progress *progress) {
     CK(cudaEventElapsedTime(&vms, v0, v1));
     s.report.ms_device = ms;
     s.report.ms_visibility = vms;
+    for (int k = 0; k < 7; ++k) {
+        float ms_k = 0.0f;
+        CK(cudaEventElapsedTime(&ms_k, s.marks[k], s.marks[k + 1]));
+        s.report.ms_stages[k] = ms_k;
+    }
     s.report.pairs = pairs;
     s.report.shadow_rays = s.counters.rays;
     s.report.burial_rays = s.counters.burial_rays;

@@ -149,13 +149,102 @@ DL_HD void sincos_d(double x, double &s, double &c) {
         default: s = -cr; c = sr; break;
     }
 }
+// ---- binary32 double-float path with a rounding test ---------------------------------------
+// GB300 runs binary64 at a small fraction of its binary32 rate, so sin/cos first run in
+// double-float binary32 arithmetic (error-free sums and FMA products; Dekker 1971, Knuth TAOCP
+// 4.2.2) to within 2^-40 of the true value, and the result is kept only when the rounding test
+// of Ziv's strategy (Ziv 1991) proves it is the correctly rounded binary32 value; otherwise the
+// binary64 path below decides. Either way the value equals what the binary64 path returns.
+struct FF {
+    float h, l;
+};
+DL_HD FF ff_two_sum(float a, float b) {
+    float s = a + b;
+    float bb = s - a;
+    return FF{s, (a - (s - bb)) + (b - bb)};
+}
+DL_HD FF ff_fast_sum(float a, float b) {
+    float s = a + b;
+    return FF{s, b - (s - a)};
+}
+DL_HD FF ff_mul(FF a, FF b) {
+    float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = e + (a.h * b.l + a.l * b.h);
+    return ff_fast_sum(p, e);
+}
+DL_HD FF ff_add(FF a, FF b) {
+    FF s = ff_two_sum(a.h, b.h);
+    return ff_fast_sum(s.h, s.l + (a.l + b.l));
+}
+DL_HD FF ff_add_f(FF a, float b) {
+    FF s = ff_two_sum(a.h, b);
+    return ff_fast_sum(s.h, s.l + a.l);
+}
+DL_HD FF ff_neg(FF a) { return FF{-a.h, -a.l}; }
+
+// sin(r) and cos(r), |r| <= pi/4, r = rh + rl: Taylor coefficients as binary32 pairs (hi + lo =
+// (-1)^n/(2n+1)! or (-1)^n/(2n)! to 48 bits) for the leading terms, single binary32 for the tail
+// terms whose share of the result is below 2^-17.
+DL_HD void ff_sincos_poly(FF r, FF &s, FF &c) {
+    FF r2 = ff_mul(r, r);
+    float z = r2.h;
+    float ts = 2.7557318844628753e-06f + z * (-2.5052107943679403e-08f + z * (1.6059044372074283e-10f +
+                                                                            z * -7.647163609812713e-13f));
+    FF p = ff_add_f(FF{-0.00019841270113829523f, 2.725596874933456e-12f}, z * ts);
+    p = ff_add(FF{0.008333333767950535f, -4.34617203337595e-10f}, ff_mul(r2, p));
+    p = ff_add(FF{-0.1666666716337204f, 4.967053879312289e-09f}, ff_mul(r2, p));
+    s = ff_add(r, ff_mul(ff_mul(r, r2), p));
+    float tc = 2.4801587642286904e-05f + z * (-2.755731998149713e-07f + z * (2.0876755879584152e-09f +
+                                                                          z * -1.147074536050896e-11f));
+    FF q = ff_add_f(FF{-0.0013888889225199819f, 3.3631094437103215e-11f}, z * tc);
+    q = ff_add(FF{0.0416666679084301f, -1.2417634698280722e-09f}, ff_mul(r2, q));
+    q = ff_add_f(ff_mul(r2, q), -0.5f);
+    c = ff_add_f(ff_mul(r2, q), 1.0f);
+}
+// Ziv's rounding test: true when every value within 2^-36 relative of h + l rounds to h.
+DL_HD bool ff_rounds_to(FF v, float &out) {
+    float a = fabsf(v.h);
+    if (!(a >= 1.0e-30f && a < 1.0e30f)) return false;
+    float up = nextafterf(v.h, INFINITY) - v.h;
+    float down = v.h - nextafterf(v.h, -INFINITY);
+    float err = a * 1.4551915228366852e-11f;  // 2^-36, far above the path's 2^-40 error bound
+    if (v.l + err < 0.5f * up && v.l - err > -0.5f * down) {
+        out = v.h;
+        return true;
+    }
+    return false;
+}
+
 DL_HD void sincos_f(float x, float &s, float &c) {
     if (!isfinite(x)) {
         s = c = NAN;
         return;
     }
+    double xd = (double)x;
+    double k = nearbyint(xd * kTwoOverPi);
+    double r = (xd - k * kPio2Hi) - k * kPio2Lo;
+    float rh = (float)r;
+    FF sv, cv;
+    ff_sincos_poly(FF{rh, (float)(r - (double)rh)}, sv, cv);
+    FF so, co;
+    switch ((long long)k & 3) {
+        case 0: so = sv; co = cv; break;
+        case 1: so = cv; co = ff_neg(sv); break;
+        case 2: so = ff_neg(sv); co = ff_neg(cv); break;
+        default: so = ff_neg(cv); co = sv; break;
+    }
+    if (x != 0.0f && ff_rounds_to(so, s) && ff_rounds_to(co, c)) return;
+    // binary64 path: the same reduction, Taylor series in binary64, one rounding
+    double sr, cr;
+    sincos_poly(r, sr, cr);
     double sd, cd;
-    sincos_d((double)x, sd, cd);
+    switch ((long long)k & 3) {
+        case 0: sd = sr; cd = cr; break;
+        case 1: sd = cr; cd = -sr; break;
+        case 2: sd = -sr; cd = -cr; break;
+        default: sd = -cr; cd = sr; break;
+    }
     s = (float)sd;
     c = (float)cd;
 }

@@ -177,6 +177,9 @@ typedef struct dl_bake_report {
     uint64_t device_bytes;    /* peak device memory held by the bake */
     uint64_t node_visits;     /* BVH nodes visited by the visibility stage (counting config only) */
     uint64_t tri_tests;       /* triangle tests of the visibility stage (counting config only) */
+    double ms_stages[8];      /* device time per stage: setup+association, texels, burial,
+                                 visibility (with its queue), bounce, optimize+seams,
+                                 serialization+crop+packing, unused */
 } dl_bake_report;
 
 /* LightBvhNode (src/bake/light_bvh.rs:16-22), 32 bytes. */

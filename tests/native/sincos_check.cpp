@@ -1,0 +1,49 @@
+// Compares the library's sin/cos (binary32 double-float path + rounding test, falling back to
+// binary64) with the binary64 path alone over many arguments; prints mismatches and the share of
+// arguments that needed the binary64 path. Built and run by tests/test_math_paths.py.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+#include "dl_math.cuh"
+
+int main(int argc, char **argv) {
+    unsigned long long n = argc > 1 ? strtoull(argv[1], nullptr, 10) : 1000000ull;
+    unsigned long long mismatch = 0, fallback = 0;
+    uint64_t state = 12345;
+    for (unsigned long long i = 0; i < n; ++i) {
+        state = dl::splitmix64(state);
+        float x;
+        switch (i % 4) {
+            case 0: x = (float)((state >> 40) * (1.0 / 16777216.0)) * 6.2831855f; break;        // [0, tau)
+            case 1: x = (float)((state >> 40) * (1.0 / 16777216.0)) * 3.1415927f - 0.78539819f; break;
+            case 2: x = (float)((state >> 40) * (1.0 / 16777216.0)) * 16.0f - 8.0f; break;
+            default: {
+                // any bit pattern with a magnitude in [2^-20, 8), either sign
+                uint32_t mant = (uint32_t)(state >> 41) & 0x7FFFFFu;
+                uint32_t ex = 107u + (uint32_t)((state >> 20) % 23u);  // exponents -20 .. 2
+                uint32_t bits = (ex << 23) | mant | ((uint32_t)(state & 1u) << 31);
+                std::memcpy(&x, &bits, 4);
+            }
+        }
+        float s, c;
+        dl::sincos_f(x, s, c);
+        double sd, cd;
+        dl::sincos_d((double)x, sd, cd);
+        float s64 = (float)sd, c64 = (float)cd;
+        if (std::memcmp(&s, &s64, 4) || std::memcmp(&c, &c64, 4)) {
+            if (mismatch < 10) std::printf("mismatch x=%a fast=(%a,%a) b64=(%a,%a)\n", x, s, c, s64, c64);
+            ++mismatch;
+        }
+        // count fallbacks by re-running the fast path's test
+        double k = nearbyint((double)x * dl::kTwoOverPi);
+        double r = ((double)x - k * dl::kPio2Hi) - k * dl::kPio2Lo;
+        float rh = (float)r;
+        dl::FF sv, cv;
+        dl::ff_sincos_poly(dl::FF{rh, (float)(r - (double)rh)}, sv, cv);
+        float t;
+        if (!dl::ff_rounds_to(sv, t) || !dl::ff_rounds_to(cv, t)) ++fallback;
+    }
+    std::printf("checked %llu mismatches %llu binary64_fallbacks %llu\n", n, mismatch, fallback);
+    return mismatch ? 1 : 0;
+}
