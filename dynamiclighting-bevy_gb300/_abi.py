@@ -67,7 +67,7 @@ class DlBakeReport(C.Structure):
                 ("bvh_nodes", C.c_uint64), ("occluders", C.c_uint64), ("h2d_bytes", C.c_uint64),
                 ("d2h_bytes", C.c_uint64), ("device_bytes", C.c_uint64),
                 ("node_visits", C.c_uint64), ("tri_tests", C.c_uint64),
-                ("ms_stages", C.c_double * 8)]
+                ("ms_stages", C.c_double * 8), ("ms_host", C.c_double * 4)]
 
 
 class DlLightBvhNode(C.Structure):

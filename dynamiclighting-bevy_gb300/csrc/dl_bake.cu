@@ -1162,6 +1162,7 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     s->options = *o;
     if (cfg) s->config = *cfg;
     std::string err;
+    auto t_prep = std::chrono::steady_clock::now();
     dl_status st = prepare_scene(*in, *o, s->host, err);
     if (st != DL_OK) {
         g_error = err;
@@ -1173,7 +1174,11 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
             g_error = "shadow maps larger than 65535 texels per side are not supported";
             return DL_UNSUPPORTED;
         }
+    s->report.ms_host[0] = ms_since(t_prep);
+    auto t_bvh = std::chrono::steady_clock::now();
     build_bvh(h);
+    s->report.ms_host[1] = ms_since(t_bvh);
+    auto t_up = std::chrono::steady_clock::now();
     // the traversal stack holds one entry per level below the root
     if (h.bvh_depth >= (uint32_t)kStack) {
         g_error = "occluder BVH deeper than the traversal stack";
@@ -1287,6 +1292,7 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     s->ctr = dev_alloc<Counters>(s->owned, 1, bytes);
     s->cancel_dev = dev_alloc<uint32_t>(s->owned, 1, bytes);
     for (auto &e : s->marks) CK(cudaEventCreate(&e));
+    s->report.ms_host[2] = ms_since(t_up);
     s->report.bvh_nodes = h.nodes.size();
     s->report.occluders = N;
     out = s.release();

@@ -8,6 +8,7 @@
 #include <cstring>
 #include <future>
 #include <numeric>
+#include <thread>
 
 namespace dl {
 
@@ -344,11 +345,13 @@ constexpr int kBins = 16;
 constexpr uint32_t kMaxLeaf = 4;
 constexpr uint32_t kMaxDepth = 60;
 
+// Subtrees larger than this, near the root, are built on their own threads.
+constexpr uint32_t kParallelPrims = 16384;
+constexpr uint32_t kParallelDepth = 6;
+
 struct Builder {
     std::vector<Prim> prims;
     std::vector<uint32_t> idx;
-    std::vector<BvhNode> nodes;
-    uint32_t max_depth = 0;
 
     static float half_area(const float lo[3], const float hi[3]) {
         float e0 = hi[0] - lo[0], e1 = hi[1] - lo[1], e2 = hi[2] - lo[2];
@@ -362,7 +365,10 @@ struct Builder {
         return r;
     }
 
-    Ref build(uint32_t first, uint32_t count, uint32_t depth) {
+    // Builds the subtree over idx[first, first + count) into `nodes`; `max_depth` collects the
+    // deepest level. The two children of a large node near the root build concurrently, the
+    // second into its own node array that is then appended with its inner references moved.
+    Ref build(std::vector<BvhNode> &nodes, uint32_t first, uint32_t count, uint32_t depth, uint32_t &max_depth) {
         max_depth = std::max(max_depth, depth);
         float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
         float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
@@ -433,8 +439,25 @@ struct Builder {
         }
         size_t node = nodes.size();
         nodes.push_back(BvhNode{});
-        Ref l = build(first, mid - first, depth + 1);
-        Ref r = build(mid, first + count - mid, depth + 1);
+        Ref l, r;
+        if (count > kParallelPrims && depth < kParallelDepth) {
+            std::vector<BvhNode> right;
+            uint32_t right_depth = 0;
+            std::thread worker([&] { r = build(right, mid, first + count - mid, depth + 1, right_depth); });
+            l = build(nodes, first, mid - first, depth + 1, max_depth);
+            worker.join();
+            int32_t base = (int32_t)nodes.size();
+            for (BvhNode nd : right) {
+                for (int c = 0; c < 2; ++c)
+                    if (nd.ref[c] >= 0) nd.ref[c] += base;
+                nodes.push_back(nd);
+            }
+            if (r.ref >= 0) r.ref += base;
+            max_depth = std::max(max_depth, right_depth);
+        } else {
+            l = build(nodes, first, mid - first, depth + 1, max_depth);
+            r = build(nodes, mid, first + count - mid, depth + 1, max_depth);
+        }
         BvhNode &n = nodes[node];
         n.c0[0] = l.lo[0]; n.c0[1] = l.hi[0]; n.c0[2] = l.lo[1]; n.c0[3] = l.hi[1];
         n.c1[0] = r.lo[0]; n.c1[1] = r.hi[0]; n.c1[2] = r.lo[1]; n.c1[3] = r.hi[1];
@@ -485,12 +508,14 @@ void build_bvh(HostScene &s) {
     }
     b.idx.resize(n);
     std::iota(b.idx.begin(), b.idx.end(), 0u);
-    b.nodes.reserve(n);
-    b.nodes.push_back(BvhNode{});  // root placeholder
-    Ref root = b.build(0, (uint32_t)n, 1);
+    std::vector<BvhNode> nodes;
+    nodes.reserve(n);
+    nodes.push_back(BvhNode{});  // root placeholder
+    uint32_t max_depth = 0;
+    Ref root = b.build(nodes, 0, (uint32_t)n, 1, max_depth);
     if (root.ref < 0) {
         // the whole set is one leaf: the root holds it and an empty second child
-        BvhNode &r = b.nodes[0];
+        BvhNode &r = nodes[0];
         r.c0[0] = root.lo[0]; r.c0[1] = root.hi[0]; r.c0[2] = root.lo[1]; r.c0[3] = root.hi[1];
         r.c2[0] = root.lo[2]; r.c2[1] = root.hi[2];
         r.c1[0] = 1e30f; r.c1[1] = -1e30f; r.c1[2] = 1e30f; r.c1[3] = -1e30f;
@@ -498,12 +523,12 @@ void build_bvh(HostScene &s) {
         r.ref[0] = root.ref; r.ref[1] = ~0; r.count[0] = 0; r.count[1] = 0;
     } else {
         // move the built root (index root.ref) into slot 0
-        b.nodes[0] = b.nodes[(size_t)root.ref];
-        for (auto &nd : b.nodes)
+        nodes[0] = nodes[(size_t)root.ref];
+        for (auto &nd : nodes)
             for (int c = 0; c < 2; ++c)
                 if (nd.ref[c] == root.ref) nd.ref[c] = 0;
     }
-    for (auto &nd : b.nodes) {
+    for (auto &nd : nodes) {
         float lo[3] = {nd.c0[0], nd.c0[2], nd.c2[0]}, hi[3] = {nd.c0[1], nd.c0[3], nd.c2[1]};
         if (nd.ref[0] != ~0) {
             pad_box(lo, hi);
@@ -515,8 +540,8 @@ void build_bvh(HostScene &s) {
             nd.c1[0] = lo1[0]; nd.c1[1] = hi1[0]; nd.c1[2] = lo1[1]; nd.c1[3] = hi1[1]; nd.c2[2] = lo1[2]; nd.c2[3] = hi1[2];
         }
     }
-    s.nodes = std::move(b.nodes);
-    s.bvh_depth = b.max_depth;
+    s.nodes = std::move(nodes);
+    s.bvh_depth = max_depth;
     for (size_t k = 0; k < n; ++k) {
         uint32_t i = b.idx[k];
         f3 a = v[i * 3], e1 = sub(v[i * 3 + 1], a), e2 = sub(v[i * 3 + 2], a);

@@ -180,6 +180,8 @@ typedef struct dl_bake_report {
     double ms_stages[8];      /* device time per stage: setup+association, texels, burial,
                                  visibility (with its queue), bounce, optimize+seams,
                                  serialization+crop+packing, unused */
+    double ms_host[4];        /* host time of session creation: validation + sorting + lights,
+                                 occluder BVH build, flattening + uploads, unused */
 } dl_bake_report;
 
 /* LightBvhNode (src/bake/light_bvh.rs:16-22), 32 bytes. */
