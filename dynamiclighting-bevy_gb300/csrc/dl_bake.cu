@@ -331,7 +331,7 @@ __device__ __forceinline__ uint32_t trace_texel(const DevScene &sc, const TraceA
 // Batched form: persistent warps pull chunks of (pair, texel) items from one queue. Items are
 // ordered sky pairs first, then soft, then hard, so the longest work starts first.
 template <bool COUNT>
-__global__ void __launch_bounds__(kBlock) k_trace_batched(DevScene sc, TraceArgs a) {
+__global__ void __launch_bounds__(kBlock, 7) k_trace_batched(DevScene sc, TraceArgs a) {
     __shared__ int stack[kStack * kBlock];
     int *my = stack + threadIdx.x;
     unsigned lane = lane_id();

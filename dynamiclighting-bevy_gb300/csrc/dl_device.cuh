@@ -153,8 +153,11 @@ __device__ bool traverse(const DevScene &sc, f3 o, f3 dir, float max, bool alpha
     bool found = false;
     int sp = 0;
     int ref = 0;
+    // while-while traversal (Aila & Laine 2009): descend inner nodes until a leaf is reached,
+    // then test leaves until an inner node comes off the stack, so a warp's lanes run the same
+    // loop body together instead of alternating node and leaf work per lane.
     for (;;) {
-        if (ref >= 0) {
+        while (ref >= 0) {
             const float4 *nd = sc.nodes + (size_t)ref * 4;
             float4 a = ldg4(nd), b = ldg4(nd + 1), c = ldg4(nd + 2), r = ldg4(nd + 3);
             if (COUNT) ++vis->nodes;
@@ -169,13 +172,14 @@ __device__ bool traverse(const DevScene &sc, f3 o, f3 dir, float max, bool alpha
                 stack[sp * stride] = swap ? r0 : r1;
                 ++sp;
                 ref = swap ? r1 : r0;
-                continue;
-            }
-            if (h0 || h1) {
+            } else if (h0 || h1) {
                 ref = h0 ? r0 : r1;
-                continue;
+            } else {
+                if (sp == 0) return found;
+                ref = stack[--sp * stride];
             }
-        } else {
+        }
+        while (ref < 0) {
             uint32_t packed = (uint32_t)(~ref);
             uint32_t first = packed >> 3, count = packed & 7u;
             for (uint32_t k = 0; k < count; ++k) {
@@ -195,10 +199,9 @@ __device__ bool traverse(const DevScene &sc, f3 o, f3 dir, float max, bool alpha
                     hit.occluder = occ;
                 }
             }
+            if (sp == 0) return found;
+            ref = stack[--sp * stride];
         }
-        if (sp == 0) return found;
-        --sp;
-        ref = stack[sp * stride];
     }
 }
 

@@ -315,8 +315,10 @@ __device__ __forceinline__ Vis sky_vis(const DevScene &sc, const DevLight &l, f3
     off.y = rng.next_f32();
     uint32_t open = 0;
     uint32_t samples = sc.sky_samples;
+    f3 side, across;
+    ortho_pair(nrm, side, across);
     for (uint32_t taken = 0; taken < samples; ++taken)
-        if (!tr(cosine_direction(nrm, spread(taken, off, true)), INFINITY)) ++open;
+        if (!tr(cosine_direction_basis(nrm, side, across, spread(taken, off, true)), INFINITY)) ++open;
     float fraction = (float)open / (float)(samples > 1 ? samples : 1);
     return Vis{true, level_of(fraction, l.shadow_bits), samples};
 }
@@ -556,8 +558,10 @@ __device__ __forceinline__ void gather_sun(const DevScene &sc, const DevLight &l
     off.y = rng.next_f32();
     uint32_t samples = l.bounce_samples;
     f3 sum{0.0f, 0.0f, 0.0f};
+    f3 side, across;
+    ortho_pair(normal, side, across);
     for (uint32_t i = 0; i < samples; ++i) {
-        f3 direction = cosine_direction(normal, spread(i, off, true));
+        f3 direction = cosine_direction_basis(normal, side, across, spread(i, off, true));
         ++rays;
         Hit h;
         if (!traverse<false>(sc, origin, direction, INFINITY, alpha, stack, stride, h)) continue;

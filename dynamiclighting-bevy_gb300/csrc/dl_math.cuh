@@ -216,35 +216,40 @@ DL_HD bool ff_rounds_to(FF v, float &out) {
     return false;
 }
 
+// pi/2 as C1 + C2 + C3 in binary32, C1 and C2 holding 21 significant bits so k * C1 and k * C2
+// are exact for the small quadrant counts k of the bake's angles (|x| < 16).
+constexpr float kPio2F1 = 1.570796012878418f;      // 0x1.921fb0p+0
+constexpr float kPio2F2 = 3.139164164167596e-07f;  // 0x1.5110b0p-22
+constexpr float kPio2F3 = 6.223371969669989e-14f;  // 0x1.184698p-44
+
 DL_HD void sincos_f(float x, float &s, float &c) {
     if (!isfinite(x)) {
         s = c = NAN;
         return;
     }
-    double xd = (double)x;
-    double k = nearbyint(xd * kTwoOverPi);
-    double r = (xd - k * kPio2Hi) - k * kPio2Lo;
-    float rh = (float)r;
-    FF sv, cv;
-    ff_sincos_poly(FF{rh, (float)(r - (double)rh)}, sv, cv);
-    FF so, co;
-    switch ((long long)k & 3) {
-        case 0: so = sv; co = cv; break;
-        case 1: so = cv; co = ff_neg(sv); break;
-        case 2: so = ff_neg(sv); co = ff_neg(cv); break;
-        default: so = ff_neg(cv); co = sv; break;
+    if (x != 0.0f && fabsf(x) < 16.0f) {
+        // Cody–Waite reduction in binary32: x - k*C1 is exact (Sterbenz), the k*C2 term enters
+        // through an error-free sum, k*C3 through the low word.
+        float k = rintf(x * 0.6366197466850281f);
+        FF r = ff_two_sum(x - k * kPio2F1, -(k * kPio2F2));
+        r = ff_fast_sum(r.h, r.l - k * kPio2F3);
+        // k = 0 needs no reduction; near-multiples of pi/2 (|r| <= 2^-16) go to binary64
+        if (k == 0.0f || fabsf(r.h) > 1.52587890625e-05f) {
+            FF sv, cv;
+            ff_sincos_poly(r, sv, cv);
+            FF so, co;
+            switch ((int)k & 3) {
+                case 0: so = sv; co = cv; break;
+                case 1: so = cv; co = ff_neg(sv); break;
+                case 2: so = ff_neg(sv); co = ff_neg(cv); break;
+                default: so = ff_neg(cv); co = sv; break;
+            }
+            if (ff_rounds_to(so, s) && ff_rounds_to(co, c)) return;
+        }
     }
-    if (x != 0.0f && ff_rounds_to(so, s) && ff_rounds_to(co, c)) return;
-    // binary64 path: the same reduction, Taylor series in binary64, one rounding
-    double sr, cr;
-    sincos_poly(r, sr, cr);
+    // binary64 path: Cody–Waite reduction and Taylor series in binary64, one rounding
     double sd, cd;
-    switch ((long long)k & 3) {
-        case 0: sd = sr; cd = cr; break;
-        case 1: sd = cr; cd = -sr; break;
-        case 2: sd = -sr; cd = -cr; break;
-        default: sd = -cr; cd = sr; break;
-    }
+    sincos_d((double)x, sd, cd);
     s = (float)sd;
     c = (float)cd;
 }
@@ -405,13 +410,16 @@ DL_HD f2 concentric(f2 sq) {
     sincos_f(angle, s, c);
     return f2{c * radius, s * radius};
 }
-// Malley's method (sky.rs:20-25).
-DL_HD f3 cosine_direction(f3 n, f2 sq) {
+// Malley's method (sky.rs:20-25), with the normal's orthonormal pair already computed.
+DL_HD f3 cosine_direction_basis(f3 n, f3 side, f3 across, f2 sq) {
     f2 d = concentric(sq);
     float up = sqrtf(fmaxf(1.0f - (d.x * d.x + d.y * d.y), 0.0f));
+    return normalize(add(add(scale(side, d.x), scale(across, d.y)), scale(n, up)));
+}
+DL_HD f3 cosine_direction(f3 n, f2 sq) {
     f3 side, across;
     ortho_pair(n, side, across);
-    return normalize(add(add(scale(side, d.x), scale(across, d.y)), scale(n, up)));
+    return cosine_direction_basis(n, side, across, sq);
 }
 
 // shadow_grid.rs:13-16

@@ -35,14 +35,14 @@ int main(int argc, char **argv) {
             if (mismatch < 10) std::printf("mismatch x=%a fast=(%a,%a) b64=(%a,%a)\n", x, s, c, s64, c64);
             ++mismatch;
         }
-        // count fallbacks by re-running the fast path's test
-        double k = nearbyint((double)x * dl::kTwoOverPi);
-        double r = ((double)x - k * dl::kPio2Hi) - k * dl::kPio2Lo;
-        float rh = (float)r;
+        // count fallbacks by re-running the fast path's reduction and test
+        float k = rintf(x * 0.6366197466850281f);
+        dl::FF r = dl::ff_two_sum(x - k * dl::kPio2F1, -(k * dl::kPio2F2));
+        r = dl::ff_fast_sum(r.h, r.l - k * dl::kPio2F3);
         dl::FF sv, cv;
-        dl::ff_sincos_poly(dl::FF{rh, (float)(r - (double)rh)}, sv, cv);
+        dl::ff_sincos_poly(r, sv, cv);
         float t;
-        if (!dl::ff_rounds_to(sv, t) || !dl::ff_rounds_to(cv, t)) ++fallback;
+        if ((k != 0.0f && fabsf(r.h) <= 1.52587890625e-05f) || !dl::ff_rounds_to(sv, t) || !dl::ff_rounds_to(cv, t)) ++fallback;
     }
     std::printf("checked %llu mismatches %llu binary64_fallbacks %llu\n", n, mismatch, fallback);
     return mismatch ? 1 : 0;
