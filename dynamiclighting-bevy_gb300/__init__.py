@@ -30,8 +30,8 @@ POINT, RECTANGLE, TUBE, SUN, SKY = 0, 1, 2, 3, 4
 DIRECT, SINGLE_BOUNCE = 0, 1
 TRANSPARENCY_DISABLED, TRANSPARENCY_ENABLED, TRANSPARENCY_ENABLED_MAX = 0, 1, 2
 LIGHTING_ONLY, DISTANCE_CUBES, ANGULAR = 0, 1, 2
-FORM_BATCHED, FORM_PLAIN = 0, 1
-FORMS = {"batched": FORM_BATCHED, "plain": FORM_PLAIN}
+FORM_BATCHED, FORM_PLAIN, FORM_REFINED = 0, 1, 2
+FORMS = {"batched": FORM_BATCHED, "plain": FORM_PLAIN, "refined": FORM_REFINED}
 
 ERROR_KINDS = {1: "Cancelled", 2: "DuplicateId", 3: "InvalidMesh", 4: "InvalidLight",
                5: "InvalidOptions"}
@@ -360,6 +360,9 @@ def load_library(path: str = LIBRARY_PATH):
     lib.dl_encode_payload.argtypes = [P(DlBakedScene), P(P(C.c_uint8)), P(C.c_uint64),
                                       P(C.c_uint32)]
     lib.dl_free.argtypes = [C.c_void_p]
+    lib.dl_session_bounce_map.restype = C.c_int
+    lib.dl_session_bounce_map.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_void_p, C.c_void_p,
+                                          C.c_uint32, P(C.c_uint32)]
     lib.dl_filter_bounce_window_noalloc.restype = C.c_int
     lib.dl_filter_bounce_window_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
                                                     C.c_uint32, C.c_uint32, C.c_void_p]
@@ -377,7 +380,7 @@ def make_config(form="batched", **tuning) -> DlBakeConfig:
     for k, v in tuning.items():
         if not hasattr(cfg, k):
             raise TypeError(f"unknown bake tuning {k!r}")
-        setattr(cfg, k, int(v))
+        setattr(cfg, k, float(v) if k == "refine_epsilon" else int(v))
     return cfg
 
 
@@ -434,6 +437,25 @@ class Session:
         r = DlBakeReport()
         self.lib.dl_session_report(self.handle, C.byref(r))
         return r
+
+    def bounce_map(self, mesh_id: int, slot: int):
+        """The last run's filtered bounce map of (mesh id, light slot) before quantization:
+        (window (min_x, min_y, max_x, max_y), float32 array [h, w, 3]), or None without one."""
+        rect = np.zeros(4, np.uint32)
+        n = C.c_uint32()
+        status = self.lib.dl_session_bounce_map(self.handle, mesh_id, slot, rect.ctypes.data, None, 0,
+                                                C.byref(n))
+        if status != 0:
+            _raise(self.lib, status)
+        if n.value == 0:
+            return None
+        rgb = np.zeros(n.value * 3, np.float32)
+        status = self.lib.dl_session_bounce_map(self.handle, mesh_id, slot, rect.ctypes.data,
+                                                rgb.ctypes.data, n.value, C.byref(n))
+        if status != 0:
+            _raise(self.lib, status)
+        w, h = int(rect[2] - rect[0] + 1), int(rect[3] - rect[1] + 1)
+        return tuple(int(x) for x in rect), rgb.reshape(h, w, 3)
 
     def close(self):
         if self.handle:

@@ -55,7 +55,7 @@ class DlBakeConfig(C.Structure):
     _fields_ = [("form", C.c_uint32), ("device", C.c_uint32), ("block_threads", C.c_uint32),
                 ("chunk_texels", C.c_uint32), ("sample_lanes", C.c_uint32),
                 ("blocks_per_sm", C.c_uint32), ("count_visits", C.c_uint32),
-                ("reserved", C.c_uint32 * 7)]
+                ("refine_epsilon", C.c_float), ("reserved", C.c_uint32 * 6)]
 
 
 class DlBakeReport(C.Structure):
@@ -67,7 +67,8 @@ class DlBakeReport(C.Structure):
                 ("bvh_nodes", C.c_uint64), ("occluders", C.c_uint64), ("h2d_bytes", C.c_uint64),
                 ("d2h_bytes", C.c_uint64), ("device_bytes", C.c_uint64),
                 ("node_visits", C.c_uint64), ("tri_tests", C.c_uint64),
-                ("ms_stages", C.c_double * 8), ("ms_host", C.c_double * 4)]
+                ("ms_stages", C.c_double * 8), ("ms_host", C.c_double * 4),
+                ("retests", C.c_uint64)]
 
 
 class DlLightBvhNode(C.Structure):
@@ -120,7 +121,7 @@ EXPORTS = [
     "dl_abi_version", "dl_status_string", "dl_last_error", "dl_bake", "dl_bake_ex",
     "dl_baked_scene_free", "dl_default_options", "dl_session_create", "dl_session_run",
     "dl_session_result", "dl_session_report", "dl_session_destroy", "dl_encode_payload",
-    "dl_free", "dl_filter_bounce_window_noalloc",
+    "dl_free", "dl_filter_bounce_window_noalloc", "dl_session_bounce_map",
 ]
 
 STATUS = {0: "ok", 1: "cancelled", 2: "duplicate id", 3: "invalid mesh", 4: "invalid light",

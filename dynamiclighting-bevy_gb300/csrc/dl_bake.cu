@@ -39,9 +39,20 @@ constexpr uint64_t kBurialStream = 0x627572696564ull;  // mesh_texels.rs:26
 struct Counters {
     unsigned long long rays, burial_rays, lights_removed, bounce_rays, photon_rays, cancelled;
     unsigned long long node_visits, tri_tests;  // instrumented visibility kernel only
+    unsigned long long retests;                 // refined form: binary64 re-tests
 };
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+// Adds a whole warp's re-test counts to the counters (every lane calls it).
+__device__ __forceinline__ void add_retests(Counters *ctr, unsigned long long n) {
+    unsigned long long w = warp_sum(n);
+    if (lane_id() == 0 && w) atomicAdd(&ctr->retests, w);
+}
 
 // ================================ setup and association ==================================
 
@@ -209,12 +220,14 @@ __global__ void k_texels(DevScene sc, const float4 *tri_face, uint32_t *owned, c
 }
 
 // Burial test per texel (mesh_texels.rs:57-88). Buried texels are dropped from tracing.
+template <bool REFINE>
 __global__ void __launch_bounds__(kBlock) k_burial(DevScene sc, uint32_t texels, const uint32_t *tex_xy,
                                                    const float4 *tex_pos, const uint32_t *tex_tri,
                                                    const float4 *tri_face, uint8_t *buried, Counters *ctr) {
     __shared__ int stack[kStack * kBlock];
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t rays = 0;
+    Visits vis{0, 0, 0};
     if (i < texels) {
         uint32_t t = tex_tri[i];
         uint32_t m = sc.tri_mesh[t];
@@ -224,10 +237,11 @@ __global__ void __launch_bounds__(kBlock) k_burial(DevScene sc, uint32_t texels,
         f3 origin = add(f3{p.x, p.y, p.z}, scale(normal, kRayOffset));
         Pcg rng = stream6(sc.seed, sc.mesh_id[m], kBurialStream, t - sc.mesh_tri_base[m], xy & 0xFFFFu, xy >> 16);
         float turn = rng.next_f32();
-        buried[i] = is_buried(sc, normal, origin, turn, stack + threadIdx.x, kBlock, rays) ? 1 : 0;
+        buried[i] = is_buried<REFINE>(sc, normal, origin, turn, stack + threadIdx.x, kBlock, rays, &vis) ? 1 : 0;
     }
     unsigned r = __reduce_add_sync(0xFFFFFFFFu, rays);
     if (lane_id() == 0 && r) atomicAdd(&ctr->burial_rays, (unsigned long long)r);
+    if (REFINE) add_retests(ctr, vis.retests);
 }
 
 __global__ void k_add_u32(const uint32_t *a, const uint32_t *b, uint32_t *c, uint32_t n) {
@@ -236,10 +250,6 @@ __global__ void k_add_u32(const uint32_t *a, const uint32_t *b, uint32_t *c, uin
     if (i == n) c[i] = 0;
 }
 
-__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
-    return v;
-}
 
 // Per triangle: how many of its texels are not buried (warp per triangle).
 template <bool WRITE>
@@ -288,7 +298,7 @@ struct TraceArgs {
 };
 
 // One (pair, texel) of the visibility loop (mesh_bake.rs:231-248); returns the rays traced.
-template <bool COUNT = false>
+template <bool COUNT = false, bool REFINE = false>
 __device__ __forceinline__ uint32_t trace_texel(const DevScene &sc, const TraceArgs &a, uint32_t p, uint32_t k,
                                                 int *stack, int stride, Visits *vis = nullptr) {
     uint32_t t = a.pair_tri[p], s = a.pair_light[p];
@@ -300,7 +310,7 @@ __device__ __forceinline__ uint32_t trace_texel(const DevScene &sc, const TraceA
     f3 pos{pp.x, pp.y, pp.z}, nrm{nn.x, nn.y, nn.z};
     f3 origin = add(pos, scale(f3{f.x, f.y, f.z}, kRayOffset));
     const DevLight &l = sc.lights[s];
-    Tracer<COUNT> tr{sc, origin, (l.flags & kLightAlpha) != 0, stack, stride, vis};
+    Tracer<COUNT, REFINE> tr{sc, origin, (l.flags & kLightAlpha) != 0, stack, stride, vis};
     Vis v = texel_shadow(sc, s, sc.mesh_id[m], x, y, pos, nrm, tr);
     if (!v.some) return 0;
     uint32_t res = sc.mesh_res[m];
@@ -330,13 +340,13 @@ __device__ __forceinline__ uint32_t trace_texel(const DevScene &sc, const TraceA
 
 // Batched form: persistent warps pull chunks of (pair, texel) items from one queue. Items are
 // ordered sky pairs first, then soft, then hard, so the longest work starts first.
-template <bool COUNT>
+template <bool COUNT, bool REFINE>
 __global__ void __launch_bounds__(kBlock, 7) k_trace_batched(DevScene sc, TraceArgs a) {
     __shared__ int stack[kStack * kBlock];
     int *my = stack + threadIdx.x;
     unsigned lane = lane_id();
     unsigned long long rays = 0;
-    Visits vis{0, 0};
+    Visits vis{0, 0, 0};
     uint32_t grabs = 0;
     for (;;) {
         unsigned long long base = 0;
@@ -358,8 +368,8 @@ __global__ void __launch_bounds__(kBlock, 7) k_trace_batched(DevScene sc, TraceA
             unsigned long long item = base + (unsigned long long)g * 32 + lane;
             if (item < a.items) {
                 while ((unsigned long long)a.item_off[cur + 1] <= item) ++cur;
-                rays += trace_texel<COUNT>(sc, a, a.order[cur], (uint32_t)(item - a.item_off[cur]), my, kBlock,
-                                           &vis);
+                rays += trace_texel<COUNT, REFINE>(sc, a, a.order[cur], (uint32_t)(item - a.item_off[cur]), my,
+                                                   kBlock, &vis);
             }
         }
     }
@@ -372,6 +382,7 @@ __global__ void __launch_bounds__(kBlock, 7) k_trace_batched(DevScene sc, TraceA
             atomicAdd(&a.ctr->tri_tests, t);
         }
     }
+    if (REFINE) add_retests(a.ctr, vis.retests);
 }
 
 // Plain form: one launch per mesh; a warp per triangle, its lights in order, lanes over texels.
@@ -425,17 +436,22 @@ __global__ void k_item_counts(const uint32_t *order, const uint32_t *pair_tri, c
 // ================================ one bounce ===========================================
 
 // PhotonCube::build (bounce.rs:48-70): every cube texel of every local bounce light.
+template <bool REFINE>
 __global__ void __launch_bounds__(kBlock) k_photons(DevScene sc, const uint32_t *cube_lights, uint32_t cubes,
-                                                    uint32_t res, Photon *photons) {
+                                                    uint32_t res, Photon *photons, Counters *ctr) {
     __shared__ int stack[kStack * kBlock];
     uint64_t per = 6ull * res * res;
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= per * cubes) return;
-    uint32_t cube = (uint32_t)(i / per);
-    uint32_t rem = (uint32_t)(i % per);
-    uint32_t face = rem / (res * res), y = (rem % (res * res)) / res, x = rem % res;
-    const DevLight &l = sc.lights[cube_lights[cube]];
-    photons[i] = make_photon(sc, l, cube_texel_direction(face, x, y, res), stack + threadIdx.x, kBlock);
+    Visits vis{0, 0, 0};
+    if (i < per * cubes) {
+        uint32_t cube = (uint32_t)(i / per);
+        uint32_t rem = (uint32_t)(i % per);
+        uint32_t face = rem / (res * res), y = (rem % (res * res)) / res, x = rem % res;
+        const DevLight &l = sc.lights[cube_lights[cube]];
+        photons[i] = make_photon<REFINE>(sc, l, cube_texel_direction(face, x, y, res), stack + threadIdx.x, kBlock,
+                                         &vis);
+    }
+    if (REFINE) add_retests(ctr, vis.retests);
 }
 
 // Pairs whose light bakes bounce, in pair order.
@@ -460,10 +476,12 @@ struct BounceArgs {
 
 // gather_triangle / gather_sun (bounce.rs:235-292, sun_bounce.rs:24-80): one thread per
 // (bounce pair, texel).
+template <bool REFINE>
 __global__ void __launch_bounds__(kBlock) k_gather(DevScene sc, BounceArgs a) {
     __shared__ int stack[kStack * kBlock];
     int *my = stack + threadIdx.x;
     unsigned long long rays = 0;
+    Visits vis{0, 0, 0};
     unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     for (unsigned long long item = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; item < a.items;
          item += stride) {
@@ -486,9 +504,9 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevScene sc, BounceArgs a) {
         uint32_t r = 0;
         bool gathered = true;
         if (l.shape == DL_SHAPE_SUN) {
-            gather_sun(sc, l, sc.mesh_id[m], xy & 0xFFFFu, xy >> 16, origin, normal, my, kBlock, v, r);
+            gather_sun<REFINE>(sc, l, sc.mesh_id[m], xy & 0xFFFFu, xy >> 16, origin, normal, my, kBlock, v, r, &vis);
         } else {
-            Tracer<false> tr{sc, origin, (l.flags & kLightAlpha) != 0, my, kBlock, nullptr};
+            Tracer<false, REFINE> tr{sc, origin, (l.flags & kLightAlpha) != 0, my, kBlock, &vis};
             gathered = gather_local(sc, l, a.photons + (size_t)l.cube * 6 * a.res * a.res, a.res, sc.mesh_id[m],
                                     xy & 0xFFFFu, xy >> 16, pos, normal, tr, v, r);
         }
@@ -497,10 +515,11 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevScene sc, BounceArgs a) {
     }
     unsigned long long sum = warp_sum(rays);
     if (lane_id() == 0 && sum) atomicAdd(&a.ctr->bounce_rays, sum);
+    if (REFINE) add_retests(a.ctr, vis.retests);
 }
 
 // The bounce window of a (mesh, light) entry: its crops' union grown by 4 (bounce_map.rs:30-43).
-__device__ __forceinline__ Rect bounce_window(const uint32_t *r, uint32_t res) {
+__host__ __device__ __forceinline__ Rect bounce_window(const uint32_t *r, uint32_t res) {
     uint32_t last = res - 1;
     return Rect{r[0] >= 4 ? r[0] - 4 : 0, r[1] >= 4 ? r[1] - 4 : 0, min(r[2] + 4, last), min(r[3] + 4, last)};
 }
@@ -1099,6 +1118,11 @@ struct dl_session {
     uint32_t *words_dev = nullptr;
     Counters counters{};
     uint64_t texels = 0;
+    // last run's filtered bounce maps: window offsets per (mesh, light) entry, RGB texels, and the
+    // entries' region rectangles (null when the run baked no bounce)
+    const uint32_t *bounce_woff = nullptr;
+    const float4 *bounce_map = nullptr;
+    const uint32_t *region_rect = nullptr;
     // batched-form graph over the visibility stage, rebuilt when the queue changes
     cudaEvent_t marks[8] = {};  // stage boundaries of the last run
     cudaGraphExec_t graph = nullptr;
@@ -1161,6 +1185,16 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     auto s = std::make_unique<dl_session>();
     s->options = *o;
     if (cfg) s->config = *cfg;
+    if (s->config.form > DL_FORM_REFINED) {
+        g_error = "unknown bake form " + std::to_string(s->config.form);
+        return DL_INVALID_ARGUMENT;
+    }
+    float eps = s->config.refine_epsilon;
+    if (!(eps >= 0.0f && eps <= 0.01f)) {
+        g_error = "refine_epsilon must lie in [0, 0.01]";
+        return DL_INVALID_ARGUMENT;
+    }
+    if (eps == 0.0f) s->config.refine_epsilon = 1.0e-5f;
     std::string err;
     auto t_prep = std::chrono::steady_clock::now();
     dl_status st = prepare_scene(*in, *o, s->host, err);
@@ -1289,6 +1323,8 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     sc.area_min_samples = o->area_light_min_samples;
     sc.sky_samples = o->sky_samples;
     sc.colored_bounce = o->colored_bounce;
+    sc.refine_eps = s->config.refine_epsilon;
+    sc.refine_eps2 = sc.refine_eps * sc.refine_eps;
     s->ctr = dev_alloc<Counters>(s->owned, 1, bytes);
     s->cancel_dev = dev_alloc<uint32_t>(s->owned, 1, bytes);
     for (auto &e : s->marks) CK(cudaEventCreate(&e));
@@ -1307,8 +1343,12 @@ dl_status run(dl_session &s, dl_progress *progress) {
     const uint32_t T = sc.triangles, M = sc.mesh_count, L = sc.light_count;
     Pool &P = s.pool;
     cudaStream_t st = s.stream;
+    const bool refine = s.config.form == DL_FORM_REFINED;
     s.launches = 0;
     s.have_result = false;
+    s.bounce_woff = nullptr;
+    s.bounce_map = nullptr;
+    s.region_rect = nullptr;
     if (progress && progress->cancel) return DL_CANCELLED;
     if (progress) {
         progress->stage = 2;  // BakeStage::Meshes (src/bake/progress.rs:8-16)
@@ -1429,8 +1469,9 @@ dl_status run(dl_session &s, dl_progress *progress) {
     }
     CK(cudaEventRecord(s.marks[2], st));
     if (texels_all) {
-        k_burial<<<grid_for(texels_all), kBlock, 0, st>>>(sc, texels_all, tex_xy, tex_pos, tex_tri, tri_face, buried,
-                                                          s.ctr);
+        auto burial = refine ? k_burial<true> : k_burial<false>;
+        burial<<<grid_for(texels_all), kBlock, 0, st>>>(sc, texels_all, tex_xy, tex_pos, tex_tri, tri_face, buried,
+                                                        s.ctr);
         LAUNCHED("k_burial");
         ++s.launches;
     }
@@ -1518,8 +1559,9 @@ dl_status run(dl_session &s, dl_progress *progress) {
         ta.grab = s.config.chunk_texels ? std::max(1u, s.config.chunk_texels / 32) : 1;
         int per_sm = 0;
         const bool count = s.config.count_visits != 0;  // instrumented variant: counts node visits
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, count ? k_trace_batched<true> : k_trace_batched<false>,
-                                                         kBlock, 0));
+        auto trace = refine ? (count ? k_trace_batched<true, true> : k_trace_batched<false, true>)
+                            : (count ? k_trace_batched<true, false> : k_trace_batched<false, false>);
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace, kBlock, 0));
         if (s.config.blocks_per_sm) per_sm = std::min(per_sm, (int)s.config.blocks_per_sm);
         unsigned blocks = (unsigned)std::max(1, per_sm * s.sms);
         // The visibility stage runs from a CUDA graph: the memset of the queue head and the
@@ -1530,8 +1572,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
             cudaGraph_t g;
             CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
             cudaMemsetAsync(head, 0, sizeof(unsigned long long), st);
-            if (items && count) k_trace_batched<true><<<blocks, kBlock, 0, st>>>(sc, ta);
-            if (items && !count) k_trace_batched<false><<<blocks, kBlock, 0, st>>>(sc, ta);
+            if (items) trace<<<blocks, kBlock, 0, st>>>(sc, ta);
             CK(cudaStreamEndCapture(st, &g));
             CK(cudaGraphInstantiate(&s.graph, g, 0));
             cudaGraphDestroy(g);
@@ -1562,7 +1603,8 @@ dl_status run(dl_session &s, dl_progress *progress) {
         if (cubes) {
             uint32_t *cube_lights = P.get<uint32_t>("cube_lights", cubes);
             CK(cudaMemcpyAsync(cube_lights, hs.cube_lights.data(), cubes * 4ull, cudaMemcpyHostToDevice, st));
-            k_photons<<<grid_for(photons_n), kBlock, 0, st>>>(sc, cube_lights, cubes, res, photons);
+            auto photon = refine ? k_photons<true> : k_photons<false>;
+            photon<<<grid_for(photons_n), kBlock, 0, st>>>(sc, cube_lights, cubes, res, photons, s.ctr);
             LAUNCHED("k_photons");
             ++s.launches;
         }
@@ -1601,9 +1643,10 @@ dl_status run(dl_session &s, dl_progress *progress) {
         ba.ctr = s.ctr;
         if (bitems) {
             int per_sm = 0;
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather, kBlock, 0));
+            auto gather = refine ? k_gather<true> : k_gather<false>;
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gather, kBlock, 0));
             unsigned blocks = (unsigned)std::min<size_t>(grid_for(bitems), (size_t)std::max(1, per_sm) * s.sms * 8);
-            k_gather<<<blocks, kBlock, 0, st>>>(sc, ba);
+            gather<<<blocks, kBlock, 0, st>>>(sc, ba);
             LAUNCHED("k_gather");
             ++s.launches;
         }
@@ -1728,10 +1771,14 @@ dl_status run(dl_session &s, dl_progress *progress) {
     s.report.bounce_rays = s.counters.bounce_rays;
     s.report.node_visits = s.counters.node_visits;
     s.report.tri_tests = s.counters.tri_tests;
+    s.report.retests = s.counters.retests;
     s.report.kernel_launches = s.launches;
     s.report.device_bytes = s.scene_bytes + P.bytes;
     s.out_words = total_words;
     s.words_dev = words;
+    s.bounce_woff = woff;
+    s.bounce_map = bmap;
+    s.region_rect = region_rect;
     s.have_result = true;
     if (progress) {
         progress->done = M;
@@ -1922,6 +1969,53 @@ dl_status dl_session_result(dl_session *s, dl_baked_scene **out) {
         dl_status st = result(*s, *out);
         s->report.ms_download = ms_since(t0);
         return st;
+    })
+}
+
+dl_status dl_session_bounce_map(dl_session *s, uint64_t mesh_id, uint32_t slot, uint32_t rect[4], float *rgb,
+                                uint32_t cap, uint32_t *texels) {
+    if (!s || !rect || !texels || (cap && !rgb)) {
+        g_error = "null argument";
+        return DL_INVALID_ARGUMENT;
+    }
+    *texels = 0;
+    if (!s->have_result) {
+        g_error = "no finished run in this session";
+        return DL_INVALID_ARGUMENT;
+    }
+    const HostScene &h = s->host;
+    uint32_t m = 0;
+    while (m < h.meshes.size() && h.meshes[m]->id != mesh_id) ++m;
+    if (m == h.meshes.size() || slot >= h.lights.size()) {
+        g_error = "no such mesh id or light slot";
+        return DL_INVALID_ARGUMENT;
+    }
+    if (!s->bounce_map || !(h.lights[slot].flags & kLightBounce)) return DL_OK;
+    DL_GUARD({
+        CK(cudaSetDevice(s->device));
+        size_t e = (size_t)m * h.lights.size() + slot;
+        uint32_t r[4];
+        uint32_t off[2];
+        CK(cudaMemcpy(r, s->region_rect + e * 4, sizeof r, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(off, s->bounce_woff + e, sizeof off, cudaMemcpyDeviceToHost));
+        if (r[0] == kNoRect) return DL_OK;
+        Rect w = bounce_window(r, h.resolution[m]);
+        rect[0] = w.min_x;
+        rect[1] = w.min_y;
+        rect[2] = w.max_x;
+        rect[3] = w.max_y;
+        uint32_t n = off[1] - off[0];
+        *texels = n;
+        if (cap) {
+            std::vector<float4> v(std::min(n, cap));
+            CK(cudaMemcpy(v.data(), s->bounce_map + off[0], v.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+            for (size_t k = 0; k < v.size(); ++k) {
+                rgb[k * 3] = v[k].x;
+                rgb[k * 3 + 1] = v[k].y;
+                rgb[k * 3 + 2] = v[k].z;
+            }
+        }
+        return DL_OK;
     })
 }
 

@@ -43,6 +43,8 @@ struct DevScene {
     uint64_t seed;
     uint32_t area_samples, area_min_samples, sky_samples;
     uint32_t colored_bounce;
+    // refined form: the epsilon of the binary64 re-test and its square
+    float refine_eps, refine_eps2;
 };
 enum : uint32_t { kMeshNormals = 1, kMeshOccludes = 2, kMeshAlpha = 4 };
 
@@ -101,10 +103,70 @@ struct Hit {
 };
 
 // Node visits and triangle tests of traversals, counted only in the instrumented kernel variant
-// the benchmark uses for its roofline bytes.
+// the benchmark uses for its roofline bytes; `retests` counts the refined form's binary64
+// re-tests.
 struct Visits {
-    unsigned long long nodes, tris;
+    unsigned long long nodes, tris, retests;
 };
+
+// The ray/triangle test of occluder `occ` in binary64 on its original vertices (the stored
+// e1/e2 are rounded binary32 differences). The operation order is intersect's; u, v and t are
+// rounded to binary32 once at the end.
+__device__ __noinline__ bool tri_test_fp64(const DevScene &sc, uint32_t occ, f3 o, f3 d, float max, float &t,
+                                           float &u, float &v) {
+    uint32_t m = sc.occ_mesh[occ];
+    const uint32_t *c = sc.indices + sc.mesh_index_base[m] + (size_t)sc.occ_tri[occ] * 3;
+    uint32_t vb = sc.mesh_vertex_base[m];
+    const float *pa = sc.positions + (size_t)(vb + c[0]) * 3, *pb = sc.positions + (size_t)(vb + c[1]) * 3,
+                *pc = sc.positions + (size_t)(vb + c[2]) * 3;
+    d3 a{pa[0], pa[1], pa[2]};
+    d3 e1 = sub(d3{pb[0], pb[1], pb[2]}, a), e2 = sub(d3{pc[0], pc[1], pc[2]}, a);
+    d3 dd = widen(d);
+    d3 p = cross(dd, e2);
+    double det = dot(e1, p);
+    if (det == 0.0 || !isfinite(det)) return false;
+    double inv = 1.0 / det;
+    d3 s = sub(widen(o), a);
+    double ud = dot(s, p) * inv;
+    if (!(ud >= 0.0 && ud <= 1.0)) return false;
+    d3 q = cross(s, e1);
+    double vd = dot(dd, q) * inv;
+    if (vd < 0.0 || ud + vd > 1.0) return false;
+    double td = dot(e2, q) * inv;
+    if (!(td >= 0.0 && td <= (double)max)) return false;
+    t = (float)td;
+    u = (float)ud;
+    v = (float)vd;
+    return true;
+}
+
+// The refined form's test: the binary32 test decides unless the ray is nearly parallel to the
+// plane (|det| <= eps |e1| |d x e2|) or u, v, u + v or t lie within eps of their bounds (t's
+// margin is eps * max(1, max) for a finite max, eps otherwise); those rays are re-tested in
+// binary64. Outside the margins the binary32 verdict and hit equal tri_test's.
+__device__ __forceinline__ bool tri_test_refined(const DevScene &sc, float4 v0, float4 e1v, float4 e2v, f3 o, f3 d,
+                                                 float max, float &t, float &u, float &v, Visits *vis) {
+    const float eps = sc.refine_eps;
+    f3 e1{e1v.x, e1v.y, e1v.z}, e2{e2v.x, e2v.y, e2v.z};
+    f3 p = cross(d, e2);
+    float det = dot(e1, p);
+    if (det * det > sc.refine_eps2 * (dot(e1, e1) * dot(p, p))) {
+        float inv = 1.0f / det;
+        f3 s{o.x - v0.x, o.y - v0.y, o.z - v0.z};
+        u = dot(s, p) * inv;
+        if (!(u >= -eps && u <= 1.0f + eps)) return false;
+        f3 q = cross(s, e1);
+        v = dot(d, q) * inv;
+        if (!(v >= -eps) || u + v > 1.0f + eps) return false;
+        t = dot(e2, q) * inv;
+        float margin = eps * (isfinite(max) ? fmaxf(max, 1.0f) : 1.0f);
+        if (!(t >= -margin && t <= max + margin)) return false;
+        bool near = u < eps || u > 1.0f - eps || v < eps || u + v > 1.0f - eps || t < margin || t > max - margin;
+        if (!near) return true;
+    }
+    ++vis->retests;
+    return tri_test_fp64(sc, __float_as_uint(v0.w), o, d, max, t, u, v);
+}
 
 constexpr int kStack = 64;  // >= BVH depth; the host refuses deeper trees
 
@@ -139,7 +201,7 @@ __device__ __forceinline__ f3 safe_inv(f3 d) {
 // memory, slots `stride` apart. For closest-hit, `hit` gets the nearest t (ties to the lowest
 // occluder index, as occluder.rs:205-210) and that test's barycentrics, which equal the ones
 // the reference recomputes with max = infinity.
-template <bool ANY, bool COUNT = false>
+template <bool ANY, bool COUNT = false, bool REFINE = false>
 __device__ bool traverse(const DevScene &sc, f3 o, f3 dir, float max, bool alpha, int *stack, int stride, Hit &hit,
                          Visits *vis = nullptr) {
     hit.t = INFINITY;
@@ -187,7 +249,10 @@ __device__ bool traverse(const DevScene &sc, f3 o, f3 dir, float max, bool alpha
                 float4 v0 = ldg4(sc.tri_v0 + i);
                 if (COUNT) ++vis->tris;
                 float t, u, v;
-                if (!tri_test(v0, ldg4(sc.tri_e1 + i), ldg4(sc.tri_e2 + i), o, d, max, t, u, v)) continue;
+                bool ok = REFINE ? tri_test_refined(sc, v0, ldg4(sc.tri_e1 + i), ldg4(sc.tri_e2 + i), o, d, max, t, u,
+                                                    v, vis)
+                                 : tri_test(v0, ldg4(sc.tri_e1 + i), ldg4(sc.tri_e2 + i), o, d, max, t, u, v);
+                if (!ok) continue;
                 uint32_t occ = __float_as_uint(v0.w);
                 if (alpha && !alpha_blocks(sc, occ, u, v)) continue;
                 if (ANY) return true;
@@ -205,11 +270,11 @@ __device__ bool traverse(const DevScene &sc, f3 o, f3 dir, float max, bool alpha
     }
 }
 
-template <bool COUNT = false>
+template <bool COUNT = false, bool REFINE = false>
 __device__ __forceinline__ bool occluded(const DevScene &sc, f3 o, f3 d, float max, bool alpha, int *stack,
                                          int stride, Visits *vis = nullptr) {
     Hit h;
-    return traverse<true, COUNT>(sc, o, d, max, alpha, stack, stride, h, vis);
+    return traverse<true, COUNT, REFINE>(sc, o, d, max, alpha, stack, stride, h, vis);
 }
 
 }  // namespace dl

@@ -174,8 +174,11 @@ struct Vis {
     uint32_t rays;
 };
 
-template <bool COUNT = false>
+// A shadow-ray tracer from one origin; REFINE selects the refined form's triangle test and
+// compensated sums in the visibility functions that use it.
+template <bool COUNT = false, bool REFINE = false>
 struct Tracer {
+    static constexpr bool kRefine = REFINE;
     const DevScene &sc;
     f3 origin;
     bool alpha;
@@ -183,13 +186,13 @@ struct Tracer {
     int stride;
     Visits *vis;
     __device__ __forceinline__ bool operator()(f3 dir, float dist) const {
-        return occluded<COUNT>(sc, origin, dir, dist, alpha, stack, stride, vis);
+        return occluded<COUNT, REFINE>(sc, origin, dir, dist, alpha, stack, stride, vis);
     }
 };
 
 // adaptive_share (area.rs:98-126); `Trace(point, w, unblocked)` is false for a point that sends
 // no light, `Point(i)` the i-th spread point.
-template <class Trace, class Point>
+template <bool KAHAN, class Trace, class Point>
 __device__ __forceinline__ bool adaptive_share(const f2 *probes, int nprobes, uint32_t samples, uint32_t minimum,
                                                Point spread_point, Trace trace, float &fraction) {
     bool any_lit = false, any_blocked = false;
@@ -201,14 +204,14 @@ __device__ __forceinline__ bool adaptive_share(const f2 *probes, int nprobes, ui
             any_blocked |= !lit;
         }
     }
-    float lit_sum = 0.0f, total = 0.0f;
+    FSum<KAHAN> lit_sum, total;
     for (uint32_t taken = 0; taken < samples; ++taken) {
         if (taken == minimum && any_lit != any_blocked) break;
         float w;
         bool unblocked;
         if (trace(spread_point(taken), w, unblocked)) {
-            total += w;
-            lit_sum += unblocked ? w : 0.0f;
+            total.add(w);
+            lit_sum.add(unblocked ? w : 0.0f);
             any_lit |= unblocked;
             any_blocked |= !unblocked;
         }
@@ -217,8 +220,8 @@ __device__ __forceinline__ bool adaptive_share(const f2 *probes, int nprobes, ui
         fraction = any_lit ? 1.0f : 0.0f;
         return true;
     }
-    if (total > 0.0f) {
-        fraction = lit_sum / total;
+    if (total.s > 0.0f) {
+        fraction = lit_sum.s / total.s;
         return true;
     }
     return false;
@@ -272,8 +275,8 @@ __device__ __forceinline__ Vis area_vis(const DevScene &sc, const DevLight &l, f
     const f2 rect_probes[5] = {{0.0f, 0.0f}, {1.0f, 0.0f}, {1.0f, 1.0f}, {0.0f, 1.0f}, {0.5f, 0.5f}};
     const f2 tube_probes[3] = {{0.0f, 0.5f}, {1.0f, 0.5f}, {0.5f, 0.5f}};
     float fraction;
-    bool some = adaptive_share(rect ? rect_probes : tube_probes, rect ? 5 : 3, sc.area_samples, sc.area_min_samples,
-                               spread_point, trace, fraction);
+    bool some = adaptive_share<TR::kRefine>(rect ? rect_probes : tube_probes, rect ? 5 : 3, sc.area_samples,
+                                            sc.area_min_samples, spread_point, trace, fraction);
     return Vis{some, some ? level_of(fraction, l.shadow_bits) : 0u, rays};
 }
 
@@ -303,7 +306,8 @@ __device__ __forceinline__ Vis sun_vis(const DevScene &sc, const DevLight &l, f3
     auto spread_point = [&](uint32_t taken) { return concentric(spread(taken, off, true)); };
     const f2 disk_probes[5] = {{0.0f, 0.0f}, {1.0f, 0.0f}, {0.0f, 1.0f}, {-1.0f, 0.0f}, {0.0f, -1.0f}};
     float fraction;
-    bool some = adaptive_share(disk_probes, 5, sc.area_samples, sc.area_min_samples, spread_point, trace, fraction);
+    bool some = adaptive_share<TR::kRefine>(disk_probes, 5, sc.area_samples, sc.area_min_samples, spread_point, trace,
+                                            fraction);
     return Vis{some, some ? level_of(fraction, l.shadow_bits) : 0u, rays};
 }
 
@@ -337,8 +341,9 @@ __device__ __forceinline__ Vis texel_shadow(const DevScene &sc, uint32_t slot, u
 
 // is_buried (mesh_texels.rs:111-135) with the back-face closest-hit test (:78-84). Returns the
 // verdict and adds the rays traced to `rays`.
+template <bool REFINE = false>
 __device__ __forceinline__ bool is_buried(const DevScene &sc, f3 normal, f3 origin, float turn, int *stack,
-                                          int stride, uint32_t &rays) {
+                                          int stride, uint32_t &rays, Visits *vis = nullptr) {
     f3 tangent, bitangent;
     ortho_pair(normal, tangent, bitangent);
     uint32_t back = 0, front = 0;
@@ -353,7 +358,7 @@ __device__ __forceinline__ bool is_buried(const DevScene &sc, f3 normal, f3 orig
         ++rays;
         Hit h;
         bool backface = false;
-        if (traverse<false>(sc, origin, dir, INFINITY, false, stack, stride, h)) {
+        if (traverse<false, false, REFINE>(sc, origin, dir, INFINITY, false, stack, stride, h, vis)) {
             // face normal of the hit occluder: cross(b - a, c - a), normalized
             float4 e1 = ldg4(sc.tri_e1 + sc.occ_leaf[h.occluder]), e2 = ldg4(sc.tri_e2 + sc.occ_leaf[h.occluder]);
             f3 fn = normalize_or_zero(cross(f3{e1.x, e1.y, e1.z}, f3{e2.x, e2.y, e2.z}));
@@ -455,9 +460,12 @@ __device__ __forceinline__ f3 hit_albedo(const DevScene &sc, const Hit &h) {
 }
 
 // photon (bounce.rs:88-115)
-__device__ __forceinline__ Photon make_photon(const DevScene &sc, const DevLight &l, f3 dir, int *stack, int stride) {
+template <bool REFINE = false>
+__device__ __forceinline__ Photon make_photon(const DevScene &sc, const DevLight &l, f3 dir, int *stack, int stride,
+                                              Visits *vis = nullptr) {
     Hit h;
-    if (!traverse<false>(sc, l.position, dir, l.radius, (l.flags & kLightAlpha) != 0, stack, stride, h))
+    if (!traverse<false, false, REFINE>(sc, l.position, dir, l.radius, (l.flags & kLightAlpha) != 0, stack, stride, h,
+                                        vis))
         return Photon{l.radius, 0u, 0u};
     f3 face = hit_face_normal(sc, h);
     f3 normal = hit_surface_normal(sc, h, face);
@@ -521,7 +529,7 @@ __device__ __forceinline__ bool gather_local(const DevScene &sc, const DevLight 
     Pcg rng = stream5(sc.seed, mesh_id, l.id, x, y);
     uint32_t samples = l.bounce_samples;
     float step = 0.9f / (float)(samples - 1);
-    f3 sum{0.0f, 0.0f, 0.0f};
+    FSum3<TR::kRefine> sum;
     for (uint32_t i = 0; i < samples; ++i) {
         float spread_s = 0.1f + (float)i * step;
         f3 random = on_unit_sphere(rng);
@@ -540,41 +548,42 @@ __device__ __forceinline__ bool gather_local(const DevScene &sc, const DevLight 
         ++rays;
         if (!tr(d, distance)) {
             float weight = fmaxf(dot(normal, d), 0.0f) * fmaxf(dot(pn, neg(d)), 0.0f);
-            sum = add(sum, scale(reflected(sc, albedo), weight));
+            sum.add(scale(reflected(sc, albedo), weight));
         }
     }
-    value = divs(scale(sum, l.bounce_intensity), (float)samples);
+    value = divs(scale(sum.value(), l.bounce_intensity), (float)samples);
     return true;
 }
 
 // gather_sun's per-texel body (sun_bounce.rs:333-370).
+template <bool REFINE = false>
 __device__ __forceinline__ void gather_sun(const DevScene &sc, const DevLight &l, uint64_t mesh_id, uint32_t x,
                                            uint32_t y, f3 origin, f3 normal, int *stack, int stride, f3 &value,
-                                           uint32_t &rays) {
+                                           uint32_t &rays, Visits *vis = nullptr) {
     bool alpha = (l.flags & kLightAlpha) != 0;
     Pcg rng = stream5(sc.seed, mesh_id, l.id, x, y);
     f2 off;
     off.x = rng.next_f32();
     off.y = rng.next_f32();
     uint32_t samples = l.bounce_samples;
-    f3 sum{0.0f, 0.0f, 0.0f};
+    FSum3<REFINE> sum;
     f3 side, across;
     ortho_pair(normal, side, across);
     for (uint32_t i = 0; i < samples; ++i) {
         f3 direction = cosine_direction_basis(normal, side, across, spread(i, off, true));
         ++rays;
         Hit h;
-        if (!traverse<false>(sc, origin, direction, INFINITY, alpha, stack, stride, h)) continue;
+        if (!traverse<false, false, REFINE>(sc, origin, direction, INFINITY, alpha, stack, stride, h, vis)) continue;
         f3 face = hit_face_normal(sc, h);
         if (dot(face, direction) >= 0.0f) continue;
         float lit = dot(hit_surface_normal(sc, h, face), l.toward);
         if (lit <= 0.0f || dot(face, l.toward) <= 0.0f) continue;
         f3 point = add(add(origin, scale(direction, h.t)), scale(face, kRayOffset));
         ++rays;
-        if (!occluded(sc, point, l.toward, INFINITY, alpha, stack, stride))
-            sum = add(sum, scale(reflected(sc, hit_albedo(sc, h)), lit));
+        if (!occluded<false, REFINE>(sc, point, l.toward, INFINITY, alpha, stack, stride, vis))
+            sum.add(scale(reflected(sc, hit_albedo(sc, h)), lit));
     }
-    value = divs(scale(sum, l.bounce_intensity), (float)samples);
+    value = divs(scale(sum.value(), l.bounce_intensity), (float)samples);
 }
 
 // quantize (bounce_pack.rs:74-86)

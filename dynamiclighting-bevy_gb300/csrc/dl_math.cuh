@@ -52,6 +52,42 @@ DL_HD f3 try_normalize(f3 a, bool &ok) {
     ok = finite_pos(r);
     return ok ? scale(a, r) : f3{0.0f, 0.0f, 0.0f};
 }
+// binary64 vectors for the refined form's ray/triangle re-test (same operation order as f3)
+struct d3 {
+    double x, y, z;
+};
+DL_HD d3 widen(f3 a) { return d3{(double)a.x, (double)a.y, (double)a.z}; }
+DL_HD d3 sub(d3 a, d3 b) { return d3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+DL_HD double dot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+DL_HD d3 cross(d3 a, d3 b) { return d3{a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
+
+// A binary32 running sum; KAHAN selects compensated summation (Kahan 1965), which the refined
+// form uses for soft-visibility weights and bounce gathers.
+template <bool KAHAN>
+struct FSum {
+    float s = 0.0f, c = 0.0f;
+    DL_HD void add(float x) {
+        if (KAHAN) {
+            float y = x - c;
+            float t = s + y;
+            c = (t - s) - y;
+            s = t;
+        } else {
+            s = s + x;
+        }
+    }
+};
+template <bool KAHAN>
+struct FSum3 {
+    FSum<KAHAN> x, y, z;
+    DL_HD void add(f3 v) {
+        x.add(v.x);
+        y.add(v.y);
+        z.add(v.z);
+    }
+    DL_HD f3 value() const { return f3{x.s, y.s, z.s}; }
+};
+
 DL_HD float fminr(float a, float b) { return fminf(a, b); }
 DL_HD float fmaxr(float a, float b) { return fmaxf(a, b); }
 DL_HD f3 vmin(f3 a, f3 b) { return f3{fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z)}; }

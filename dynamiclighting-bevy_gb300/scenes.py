@@ -337,17 +337,15 @@ def _fbm(seed, n, octaves=6):
     return (h - h.min()) / max(h.max() - h.min(), 1e-9)
 
 
-def outdoor(seed=4, grid=512, chunks=8, boxes=2000, point_lights=32, density=4.0,
-            sun_samples=32, sky_samples=256, bounce_samples=128):
-    """512x512-vertex heightfield (heights 0..40 m, 1 m spacing) in 8x8 chunk meshes, 2000
-    boxes and 0.02 m planks, a 0.53 deg sun (4-bit, 32 samples, colored bounce with 128
-    samples), a sky (256 samples) and 32 point lights of radius U[4, 12], 4 texels/m."""
-    rng = Rng(seed)
+def _terrain(seed, grid, chunks, rng, first_id=1):
+    """fBm heightfield (0..40 m, 1 m spacing) as chunks x chunks meshes facing +y; returns
+    (meshes, heights)."""
     heights = (_fbm(seed, grid) * 40.0)
     size = float(grid - 1)
     meshes = []
     per = (grid - 1) // chunks
-    mesh_id = 1
+    mesh_id = first_id
+    gx_all, gz_all = np.gradient(heights, axis=1), np.gradient(heights, axis=0)
     for cz in range(chunks):
         for cx in range(chunks):
             x0, z0 = cx * per, cz * per
@@ -358,8 +356,8 @@ def outdoor(seed=4, grid=512, chunks=8, boxes=2000, point_lights=32, density=4.0
             H = heights[z0:z1 + 1, x0:x1 + 1]
             pos = np.stack([X - size / 2, H, Z - size / 2], -1).reshape(-1, 3)
             # central-difference normals
-            gx = np.gradient(heights, axis=1)[z0:z1 + 1, x0:x1 + 1]
-            gz = np.gradient(heights, axis=0)[z0:z1 + 1, x0:x1 + 1]
+            gx = gx_all[z0:z1 + 1, x0:x1 + 1]
+            gz = gz_all[z0:z1 + 1, x0:x1 + 1]
             nrm = np.stack([-gx, np.ones_like(gx), -gz], -1)
             nrm /= np.linalg.norm(nrm, axis=-1, keepdims=True)
             w, h = x1 - x0 + 1, z1 - z0 + 1
@@ -374,6 +372,18 @@ def outdoor(seed=4, grid=512, chunks=8, boxes=2000, point_lights=32, density=4.0
                                    normals=nrm.reshape(-1, 3).astype(np.float32), albedo=col,
                                    content_hash=splitmix64(mesh_id)))
             mesh_id += 1
+    return meshes, heights
+
+
+def outdoor(seed=4, grid=512, chunks=8, boxes=2000, point_lights=32, density=4.0,
+            sun_samples=32, sky_samples=256, bounce_samples=128):
+    """512x512-vertex heightfield (heights 0..40 m, 1 m spacing) in 8x8 chunk meshes, 2000
+    boxes and 0.02 m planks, a 0.53 deg sun (4-bit, 32 samples, colored bounce with 128
+    samples), a sky (256 samples) and 32 point lights of radius U[4, 12], 4 texels/m."""
+    rng = Rng(seed)
+    meshes, heights = _terrain(seed, grid, chunks, rng)
+    size = float(grid - 1)
+    mesh_id = len(meshes) + 1
 
     def ground(x, z):
         i = int(np.clip(round(z + size / 2), 0, grid - 1))
@@ -408,9 +418,123 @@ def outdoor(seed=4, grid=512, chunks=8, boxes=2000, point_lights=32, density=4.0
     return BakeInput(meshes, ls), opts
 
 
+# ---- workload 5: precision stress ---------------------------------------------------------
+
+def _atlas_triangles(mesh_id, corners, quads, albedo, occludes=True):
+    """A mesh of n independent quads (corners (n, 4, 3), as two triangles 0-1-2, 0-2-3) or
+    triangles (n, 3, 3), each in its own cell of a square UV1 atlas (0.9 scale, 0.05 margin)."""
+    n, k = corners.shape[0], corners.shape[1]
+    cells = math.ceil(math.sqrt(n))
+    cell = np.stack([np.arange(n) % cells, np.arange(n) // cells], -1).astype(np.float64)
+    unit = np.array([[0, 0], [1, 0], [1, 1], [0, 1]] if quads else [[0, 0], [1, 0], [0, 1]], np.float64)
+    uv = (cell[:, None, :] + unit[None, :, :] * 0.9 + 0.05) / cells
+    base = (np.arange(n) * k)[:, None]
+    local = np.array([0, 1, 2, 0, 2, 3] if quads else [0, 1, 2])
+    idx = (base + local[None, :]).reshape(-1)
+    return BakeMesh(id=mesh_id, positions=corners.reshape(-1, 3).astype(np.float32),
+                    indices=idx.astype(np.uint32), uv1=uv.reshape(-1, 2).astype(np.float32),
+                    albedo=albedo, occludes=occludes, content_hash=splitmix64(mesh_id ^ n))
+
+
+def precision_stress(seed=5, grid=1024, chunks=16, boxes=2000, decals=200_000, slivers=20_000,
+                     lights=256, density=4.0, area_samples=32, sky_samples=256, bounce_samples=128,
+                     decal_lift=1.0e-4, per_mesh=800):
+    """The outdoor scene at grid x grid vertices (1024: 2.09 M terrain triangles) plus `decals`
+    quads lying on terrain triangles lifted `decal_lift` m along their normal, `slivers` standing
+    triangles of aspect ratio log-uniform in [10, 1e4] (1..4 m long), boxes and planks, and
+    `lights` mixed lights: a sun (0.53 deg, colored bounce), a sky, then half point lights and a
+    quarter each rectangles and tubes, radius U[4, 12]."""
+    rng = Rng(seed)
+    meshes, heights = _terrain(seed, grid, chunks, rng)
+    size = float(grid - 1)
+    mesh_id = len(meshes) + 1
+    half = size / 2
+
+    def vertex(i, j):  # heightfield vertex at row i (z), column j (x), float64
+        return np.stack([j - half, heights[i, j], i - half], -1).astype(np.float64)
+
+    # decals: a kite inside a terrain triangle (barycentric corners), lifted along its normal
+    cell_i = (hashed_uniform(seed * 7 + 1, decals) * (grid - 1)).astype(np.int64)
+    cell_j = (hashed_uniform(seed * 7 + 2, decals) * (grid - 1)).astype(np.int64)
+    upper = hashed_uniform(seed * 7 + 3, decals) < 0.5
+    a = vertex(cell_i, cell_j)
+    b = vertex(cell_i, cell_j + 1)
+    c = vertex(cell_i + 1, cell_j + 1)
+    d = vertex(cell_i + 1, cell_j)
+    # the terrain's triangles are (a, d, c) and (a, c, b)
+    p0, p1, p2 = a, np.where(upper[:, None], d, c), np.where(upper[:, None], c, b)
+    n = np.cross(p1 - p0, p2 - p0)
+    n /= np.linalg.norm(n, axis=-1, keepdims=True)
+    kite = np.array([[0.15, 0.15], [0.65, 0.15], [0.42, 0.42], [0.15, 0.65]])
+    corners = (p0[:, None, :] + kite[None, :, 0:1] * (p1 - p0)[:, None, :]
+               + kite[None, :, 1:2] * (p2 - p0)[:, None, :] + decal_lift * n[:, None, :])
+    for start in range(0, decals, per_mesh):
+        meshes.append(_atlas_triangles(mesh_id, corners[start:start + per_mesh], True,
+                                       (rng.uniform(0.2, 0.8), rng.uniform(0.2, 0.8), rng.uniform(0.2, 0.8))))
+        mesh_id += 1
+
+    # slivers: standing triangles, long edge L, base width L / aspect
+    if slivers:
+        x = (hashed_uniform(seed * 7 + 4, slivers) - 0.5) * (size - 8)
+        z = (hashed_uniform(seed * 7 + 5, slivers) - 0.5) * (size - 8)
+        i = np.clip(np.round(z + half).astype(np.int64), 0, grid - 1)
+        j = np.clip(np.round(x + half).astype(np.int64), 0, grid - 1)
+        base = np.stack([x, heights[i, j] - 0.05, z], -1)
+        length = 1.0 + 3.0 * hashed_uniform(seed * 7 + 6, slivers)
+        aspect = 10.0 ** (1.0 + 3.0 * hashed_uniform(seed * 7 + 7, slivers))
+        turn = hashed_uniform(seed * 7 + 8, slivers) * 2 * math.pi
+        lean = (hashed_uniform(seed * 7 + 9, slivers) - 0.5) * 0.6
+        side = np.stack([np.cos(turn), np.zeros_like(turn), np.sin(turn)], -1)
+        up = np.stack([-np.sin(turn) * lean, np.ones_like(turn), np.cos(turn) * lean], -1)
+        up /= np.linalg.norm(up, axis=-1, keepdims=True)
+        tri = np.stack([base, base + side * (length / aspect)[:, None], base + up * length[:, None]], 1)
+        for start in range(0, slivers, per_mesh):
+            meshes.append(_atlas_triangles(mesh_id, tri[start:start + per_mesh], False, (0.6, 0.6, 0.5)))
+            mesh_id += 1
+
+    def ground(x, z):
+        i = int(np.clip(round(z + half), 0, grid - 1))
+        j = int(np.clip(round(x + half), 0, grid - 1))
+        return float(heights[i, j])
+
+    for k in range(boxes):
+        x, z = rng.uniform(-half + 4, half - 4), rng.uniform(-half + 4, half - 4)
+        y = ground(x, z) - 0.2
+        col = (rng.uniform(0.2, 0.8), rng.uniform(0.2, 0.8), rng.uniform(0.2, 0.8))
+        if k % 4 == 3:
+            lx, lz = rng.uniform(1.0, 3.0), rng.uniform(0.2, 0.6)
+            y += rng.uniform(0.5, 2.0)
+            parts = box_parts((x, y, z), (x + lx, y + 0.02, z + lz))
+        else:
+            e = (rng.uniform(0.5, 3.0), rng.uniform(0.5, 3.0), rng.uniform(0.5, 3.0))
+            parts = box_parts((x, y, z), (x + e[0], y + e[1], z + e[2]))
+        meshes.append(atlas_mesh(mesh_id, parts, col))
+        mesh_id += 1
+
+    sun = rotation_arc((0, 0, 1), (0.35, 1.0, 0.25))
+    ls = [BakeLight(id=30_000, position=(0.0, 0.0, 0.0), radius=1.0, illumination=SINGLE_BOUNCE,
+                    bounce=BakeBounce(samples=bounce_samples), shape=LightShape.sun(sun, 0.53)),
+          BakeLight(id=30_001, position=(0.0, 0.0, 0.0), radius=1.0, shape=LightShape.sky())]
+    local = max(lights - 2, 0)
+    for k in range(local):
+        x, z = rng.uniform(-half + 2, half - 2), rng.uniform(-half + 2, half - 2)
+        pos = (x, ground(x, z) + rng.uniform(1.0, 5.0), z)
+        shape = LightShape.point()
+        if k % 4 == 2:
+            rot = quat_mul(rotation_y(rng.uniform(0, 2 * math.pi)), rotation_x(-math.pi / 2))
+            shape = LightShape.rectangle(rot, rng.uniform(0.5, 3.0), rng.uniform(0.5, 3.0))
+        elif k % 4 == 3:
+            shape = LightShape.tube(rotation_y(rng.uniform(0, 2 * math.pi)), rng.uniform(1.0, 4.0))
+        ls.append(BakeLight(id=20_000 + k, position=pos, radius=rng.uniform(4.0, 12.0), shape=shape))
+    opts = _options(pixel_density=density, area_light_samples=area_samples,
+                    area_light_min_samples=16, sky_samples=sky_samples, colored_bounce=True)
+    return BakeInput(meshes, ls), opts
+
+
 WORKLOADS = {
     "small_room": small_room,
     "room_grid": room_grid,
     "soft_rooms": soft_rooms,
     "outdoor": outdoor,
+    "precision_stress": precision_stress,
 }

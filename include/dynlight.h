@@ -135,12 +135,18 @@ typedef struct dl_progress {
     volatile uint64_t total;
 } dl_progress;
 
-/* How the visibility stage runs. Both forms give identical bytes. */
+/* How the bake runs. BATCHED and PLAIN give identical bytes, bit-exact with the reference's
+   binary32 arithmetic. REFINED is the batched form with two precision changes: ray/triangle tests
+   whose binary32 barycentrics, determinant or hit distance fall within `refine_epsilon` of a
+   boundary are re-tested in binary64, and soft-visibility weights and bounce gathers are summed
+   with compensated (Kahan) sums. Its bytes may differ from the other forms where those re-tests
+   or sums change a level. */
 enum {
     DL_FORM_BATCHED = 0, /* every (triangle, light) pair through one persistent kernel fed by a
                             device work queue, launched from a CUDA graph */
-    DL_FORM_PLAIN = 1    /* one launch per mesh, a warp per triangle looping over its lights and
+    DL_FORM_PLAIN = 1,   /* one launch per mesh, a warp per triangle looping over its lights and
                             texels: the reference's loop order on the GPU */
+    DL_FORM_REFINED = 2  /* the batched form with binary64 edge re-tests and compensated sums */
 };
 
 /* Launch configuration of one bake; zero-initialise for the defaults. */
@@ -153,7 +159,9 @@ typedef struct dl_bake_config {
     uint32_t blocks_per_sm;    /* persistent blocks per SM, 0: default */
     uint32_t count_visits;     /* 1: run the instrumented visibility kernel that counts BVH node
                                   visits and triangle tests (for roofline accounting; slower) */
-    uint32_t reserved[7];
+    float refine_epsilon;      /* DL_FORM_REFINED: re-test margin (barycentric units; times
+                                  max(1, ray length) for distances), 0: 1e-5 */
+    uint32_t reserved[6];
 } dl_bake_config;
 
 /* Timings (device events, milliseconds) and counters of the last bake. */
@@ -182,6 +190,7 @@ typedef struct dl_bake_report {
                                  serialization+crop+packing, unused */
     double ms_host[4];        /* host time of session creation: validation + sorting + lights,
                                  occluder BVH build, flattening + uploads, unused */
+    uint64_t retests;         /* DL_FORM_REFINED: ray/triangle tests re-run in binary64 */
 } dl_bake_report;
 
 /* LightBvhNode (src/bake/light_bvh.rs:16-22), 32 bytes. */
@@ -288,6 +297,13 @@ dl_status dl_session_run(dl_session *session, dl_progress *progress);
 /* Downloads the last run's results and serializes them. */
 dl_status dl_session_result(dl_session *session, dl_baked_scene **out);
 dl_status dl_session_report(const dl_session *session, dl_bake_report *report);
+/* No counterpart in the reference (whose BounceMap is internal to bake_mesh_bounce,
+   src/bake/bounce.rs:155-217): the last run's filtered bounce map of (mesh id, light slot) —
+   its window (min_x, min_y, max_x, max_y) and up to `cap` RGB texels row-major over the window,
+   before quantization. `*texels` gets the window's texel count, 0 when the pair has no map.
+   For precision reports of bounce irradiance. */
+dl_status dl_session_bounce_map(dl_session *session, uint64_t mesh_id, uint32_t slot, uint32_t rect[4],
+                                float *rgb, uint32_t cap, uint32_t *texels);
 void dl_session_destroy(dl_session *session);
 
 /* ---- .dynlight payload (src/bake/format/mod.rs:101-213): the uncompressed payload bytes and

@@ -45,7 +45,22 @@ def lib():
         _lib.oracle_intersect.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
                                           C.c_void_p, C.c_void_p]
         _lib.oracle_slerp.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p]
+        _lib.oracle_bake_ex.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                        C.c_uint32, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p]
+        _lib.oracle_intersect_batch.restype = C.c_uint64
+        _lib.oracle_intersect_batch.argtypes = [C.c_uint32, C.c_float, C.c_uint32] + [C.c_void_p] * 6
+        _lib.oracle_captured_map.restype = C.c_uint32
+        _lib.oracle_captured_map.argtypes = [C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.c_uint32]
+        _lib.oracle_captured_map_count.restype = C.c_uint32
+        _lib.oracle_capture_all_bounce.argtypes = [C.c_uint32]
     return _lib
+
+
+# Precision modes of bake_ex: the reference's binary32, the GPU library's refined form, and the
+# FP64 oracle (binary64 ray/triangle tests, sums and fractions over the same binary32 samples).
+F32, REFINED, F64 = 0, 1, 2
 
 
 DIR_FN = C.CFUNCTYPE(C.c_int, C.POINTER(C.c_float), C.c_float)
@@ -77,3 +92,49 @@ def bake(inp, options, threads=0, brute_force=False, progress=None):
         return dl.scene_from_c(out.contents), burial.value, photon.value
     finally:
         lb.oracle_free(out)
+
+
+def bake_ex(inp, options, mode=F32, eps=1.0e-5, threads=0, brute_force=False, bounce_maps=False):
+    """Runs the oracle bake in precision `mode`. Returns a dict with the BakedScene ("scene"),
+    "burial_rays", "photon_rays", "retests" and, with bounce_maps, every filtered bounce map as
+    {(mesh id, slot): (window, float32 [h, w, 3])} under "maps"."""
+    import dynlight_gb300 as dl
+    m = dl.Marshalled(inp)
+    opts = dl.marshal_options(options)
+    out = C.POINTER(dl._abi.DlBakedScene)()
+    burial, photon, retests = C.c_uint64(), C.c_uint64(), C.c_uint64()
+    lb = lib()
+    lb.oracle_capture_all_bounce(1 if bounce_maps else 0)
+    status = lb.oracle_bake_ex(C.byref(m.input), C.byref(opts), None, threads, 1 if brute_force else 0,
+                               mode, eps, C.byref(out), C.byref(burial), C.byref(photon),
+                               C.byref(retests))
+    maps = {}
+    if bounce_maps:
+        mid, slot = C.c_uint64(), C.c_uint32()
+        rect = np.zeros(4, np.uint32)
+        for i in range(lb.oracle_captured_map_count()):
+            n = lb.oracle_captured_map(i, C.byref(mid), C.byref(slot), rect.ctypes.data, None, 0)
+            rgb = np.zeros(n * 3, np.float32)
+            lb.oracle_captured_map(i, C.byref(mid), C.byref(slot), rect.ctypes.data, rgb.ctypes.data, n)
+            w, h = int(rect[2] - rect[0] + 1), int(rect[3] - rect[1] + 1)
+            maps[(mid.value, slot.value)] = (tuple(int(x) for x in rect), rgb.reshape(h, w, 3))
+        lb.oracle_capture_all_bounce(0)
+    if status != 0:
+        raise dl.BakeError(status, (lb.oracle_last_error() or b"").decode())
+    try:
+        scene = dl.scene_from_c(out.contents)
+    finally:
+        lb.oracle_free(out)
+    return {"scene": scene, "burial_rays": burial.value, "photon_rays": photon.value,
+            "retests": retests.value, "maps": maps}
+
+
+def intersect_batch(mode, eps, tris, origins, dirs, max_t):
+    """Ray/triangle tests in precision `mode`: (hit bool[n], t float32[n], retests)."""
+    tris = f32(tris)
+    n = tris.size // 9
+    o, d, mx = f32(origins), f32(dirs), f32(max_t)
+    hit = np.zeros(n, np.uint8)
+    t = np.zeros(n, np.float32)
+    r = lib().oracle_intersect_batch(mode, eps, n, ptr(tris), ptr(o), ptr(d), ptr(mx), ptr(hit), ptr(t))
+    return hit.astype(bool), t, r

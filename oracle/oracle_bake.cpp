@@ -348,7 +348,7 @@ static Traced trace(const Scene &sc, const Prepared &p, const std::vector<Setup>
                 if (!v.some) continue;
                 r += v.rays;
                 tr.visited.set_atomic(texel.x, texel.y);
-                grid.grid.raise_atomic(texel.x - rect.min_x, texel.y - rect.min_y, level(v.fraction, bits));
+                grid.grid.raise_atomic(texel.x - rect.min_x, texel.y - rect.min_y, level_of(v.fraction, bits));
             }
         }
         texels += tx.size();
@@ -384,7 +384,7 @@ static uint64_t gather_triangle(const Scene &sc, const std::vector<SurfaceTexel>
         V3 origin = tx.position + normal * RAY_OFFSET;
         uint64_t parts[5] = {sc.options->seed, p.mesh->id, light.l->id, tx.x, tx.y};
         Rng rng = stream(parts, 5);
-        V3 sum{0, 0, 0};
+        Acc3 sum;
         for (uint32_t i = 0; i < samples; ++i) {
             float spread_s = 0.1f + (float)i * spread_step;
             V3 random = on_unit_sphere(rng);
@@ -398,10 +398,10 @@ static uint64_t gather_triangle(const Scene &sc, const std::vector<SurfaceTexel>
             ++rays;
             if (!sc.occluders.occluded(origin, d, distance, alpha)) {
                 float weight = fmax_r(dot(normal, d), 0.0f) * fmax_r(dot(pn, -d), 0.0f);
-                sum = sum + reflected(sc, albedo) * weight;
+                sum.add(reflected(sc, albedo) * weight);
             }
         }
-        out.push_back(GatheredTexel{tx.x, tx.y, sum * light.l->bounce_intensity / (float)samples});
+        out.push_back(GatheredTexel{tx.x, tx.y, sum.mean(light.l->bounce_intensity, samples)});
     }
     return rays;
 }
@@ -423,7 +423,7 @@ static uint64_t gather_sun(const Scene &sc, const std::vector<SurfaceTexel> &tex
         V2 offset;
         offset.x = rng.next_f32();
         offset.y = rng.next_f32();
-        V3 sum{0, 0, 0};
+        Acc3 sum;
         for (uint32_t i = 0; i < samples; ++i) {
             V3 direction = cosine_direction(normal, spread(i, offset, true));
             ++rays;
@@ -435,9 +435,9 @@ static uint64_t gather_sun(const Scene &sc, const std::vector<SurfaceTexel> &tex
             if (lit <= 0.0f || dot(face, toward) <= 0.0f) continue;
             V3 point = origin + direction * hit.distance + face * RAY_OFFSET;
             ++rays;
-            if (!occ.occluded(point, toward, INFINITY, alpha)) sum = sum + reflected(sc, occ.albedo(hit)) * lit;
+            if (!occ.occluded(point, toward, INFINITY, alpha)) sum.add(reflected(sc, occ.albedo(hit)) * lit);
         }
-        out.push_back(GatheredTexel{tx.x, tx.y, sum * light.l->bounce_intensity / (float)samples});
+        out.push_back(GatheredTexel{tx.x, tx.y, sum.mean(light.l->bounce_intensity, samples)});
     }
     return rays;
 }
@@ -453,6 +453,18 @@ struct BounceCapture {
     std::vector<V3> pre, post;
 };
 static BounceCapture g_capture;
+// All filtered bounce maps of the next bake, when armed (for precision reports).
+struct CapturedMap {
+    uint64_t mesh_id;
+    uint32_t slot;
+    Rect rect;
+    std::vector<V3> post;
+};
+static struct {
+    bool on = false;
+    std::mutex lock;
+    std::vector<CapturedMap> maps;
+} g_capture_all;
 
 // bake_mesh_bounce (bounce.rs:155-217): result[t][k] = padded bounce grid or empty.
 static uint64_t mesh_bounce(const Scene &sc, const Prepared &p, const std::vector<Setup> &setups,
@@ -505,6 +517,10 @@ static uint64_t mesh_bounce(const Scene &sc, const Prepared &p, const std::vecto
         map.dilate();
         map.blur();
         if (capture) g_capture.post = map.values;
+        if (g_capture_all.on) {
+            std::lock_guard<std::mutex> guard(g_capture_all.lock);
+            g_capture_all.maps.push_back(CapturedMap{p.mesh->id, slot, map.rect, map.values});
+        }
         for (auto &r : receivers) has[r.first][r.second] = map.crop(setups[r.first].crop, result[r.first][r.second]);
     }
     return rays;
@@ -873,12 +889,27 @@ static thread_local std::string g_error;
 const char *oracle_last_error(void) { return g_error.c_str(); }
 
 // Bakes with `threads` worker threads (0: all cores). `brute_force` tests every occluder per ray.
-int oracle_bake(const dl_bake_input *in, const dl_bake_options *o, const dl_progress *progress, uint32_t threads,
-                uint32_t brute_force, dl_baked_scene **out, uint64_t *burial_rays, uint64_t *photon_rays) {
+// `mode` is a Precision (0 the reference's binary32, 1 the refined form with re-test margin
+// `eps`, 2 the FP64 oracle); `retests` gets the refined form's binary64 re-tests.
+int oracle_bake_ex(const dl_bake_input *in, const dl_bake_options *o, const dl_progress *progress, uint32_t threads,
+                   uint32_t brute_force, uint32_t mode, float eps, dl_baked_scene **out, uint64_t *burial_rays,
+                   uint64_t *photon_rays, uint64_t *retests) {
+    if (mode > PREC_F64 || !(eps >= 0.0f)) {
+        g_error = "invalid precision mode";
+        *out = nullptr;
+        return DL_INVALID_OPTIONS;
+    }
     thread_count() = threads ? threads : std::max(1u, std::thread::hardware_concurrency());
+    precision().mode = (Precision)mode;
+    precision().eps = eps;
+    precision().eps2 = eps * eps;
+    retest_count().store(0);
     auto *res = new Result();
     Error err{DL_OK, ""};
-    if (!bake(*in, *o, progress, brute_force != 0, *res, err)) {
+    bool ok = bake(*in, *o, progress, brute_force != 0, *res, err);
+    precision() = PrecisionMode{};
+    if (retests) *retests = retest_count().load();
+    if (!ok) {
         g_error = err.message;
         delete res;
         *out = nullptr;
@@ -890,7 +921,37 @@ int oracle_bake(const dl_bake_input *in, const dl_bake_options *o, const dl_prog
     *out = &res->scene;
     return DL_OK;
 }
+int oracle_bake(const dl_bake_input *in, const dl_bake_options *o, const dl_progress *progress, uint32_t threads,
+                uint32_t brute_force, dl_baked_scene **out, uint64_t *burial_rays, uint64_t *photon_rays) {
+    return oracle_bake_ex(in, o, progress, threads, brute_force, PREC_F32, 0.0f, out, burial_rays, photon_rays,
+                          nullptr);
+}
 void oracle_free(dl_baked_scene *s) { delete reinterpret_cast<Result *>(s); }
+
+// Arms (on = 1) or clears the capture of every filtered bounce map of the next bakes.
+void oracle_capture_all_bounce(uint32_t on) {
+    std::lock_guard<std::mutex> guard(g_capture_all.lock);
+    g_capture_all.on = on != 0;
+    g_capture_all.maps.clear();
+}
+uint32_t oracle_captured_map_count(void) { return (uint32_t)g_capture_all.maps.size(); }
+// Map i: its mesh id, light slot, window (min_x, min_y, max_x, max_y) and up to `cap` RGB
+// texels row-major over the window; returns the window's texel count.
+uint32_t oracle_captured_map(uint32_t i, uint64_t *mesh_id, uint32_t *slot, uint32_t rect[4], float *rgb,
+                             uint32_t cap) {
+    if (i >= g_capture_all.maps.size()) return 0;
+    const CapturedMap &m = g_capture_all.maps[i];
+    *mesh_id = m.mesh_id;
+    *slot = m.slot;
+    rect[0] = m.rect.min_x; rect[1] = m.rect.min_y; rect[2] = m.rect.max_x; rect[3] = m.rect.max_y;
+    uint32_t n = (uint32_t)m.post.size();
+    for (uint32_t k = 0; k < n && k < cap; ++k) {
+        rgb[k * 3] = m.post[k].x;
+        rgb[k * 3 + 1] = m.post[k].y;
+        rgb[k * 3 + 2] = m.post[k].z;
+    }
+    return n;
+}
 
 // Arms the bounce-map capture of (mesh id, light slot) for the next oracle_bake.
 void oracle_capture_bounce(uint64_t mesh_id, uint32_t slot) {
@@ -1042,6 +1103,27 @@ int oracle_intersect(const float v[9], const float o[3], const float d[3], float
     bool hit = intersect(vv, V3{o[0], o[1], o[2]}, V3{d[0], d[1], d[2]}, max, *t, ww);
     if (hit) { w[0] = ww.x; w[1] = ww.y; w[2] = ww.z; }
     return hit;
+}
+// n ray/triangle tests in precision `mode` (re-test margin `eps`): triangle i is v[9i..9i+9],
+// ray i o[3i..], d[3i..] with length max[i]; hit[i] gets 1/0 and t[i] the distance of a hit.
+// Returns the refined mode's binary64 re-tests.
+uint64_t oracle_intersect_batch(uint32_t mode, float eps, uint32_t n, const float *v, const float *o, const float *d,
+                                const float *max, uint8_t *hit, float *t) {
+    precision().mode = (Precision)std::min<uint32_t>(mode, PREC_F64);
+    precision().eps = eps;
+    precision().eps2 = eps * eps;
+    retest_count().store(0);
+    for (uint32_t i = 0; i < n; ++i) {
+        const float *a = v + (size_t)i * 9;
+        V3 vv[3] = {{a[0], a[1], a[2]}, {a[3], a[4], a[5]}, {a[6], a[7], a[8]}};
+        V3 w;
+        float ti = 0.0f;
+        hit[i] = intersect(vv, V3{o[i * 3], o[i * 3 + 1], o[i * 3 + 2]}, V3{d[i * 3], d[i * 3 + 1], d[i * 3 + 2]},
+                           max[i], ti, w);
+        t[i] = hit[i] ? ti : 0.0f;
+    }
+    precision() = PrecisionMode{};
+    return retest_count().load();
 }
 // Area-light visibility of one texel with a callback `blocked(dir, distance)`; the shape is the
 // light's rotation and size at `center`. Returns 1 with fraction/rays, or 0 for None.

@@ -151,7 +151,7 @@ inline V3 cosine_direction(V3 normal, V2 square) {
 // ---- visibility (src/bake/area.rs, sun.rs, sky.rs, texel_shadow.rs) -------------------------------
 struct Visibility {
     bool some;
-    float fraction;
+    double fraction;  // binary32 values except in the F64 mode
     uint32_t rays;
 };
 struct Sampling {
@@ -162,7 +162,7 @@ struct Sampling {
 // that sends no light.
 template <class P, class SpreadPoint, class Trace>
 inline bool adaptive_share(const P *probes, int probe_count, Sampling s, SpreadPoint spread_point, Trace trace,
-                           float &fraction) {
+                           double &fraction) {
     bool any_lit = false, any_blocked = false;
     for (int i = 0; i < probe_count; ++i) {
         float w;
@@ -172,24 +172,24 @@ inline bool adaptive_share(const P *probes, int probe_count, Sampling s, SpreadP
             any_blocked |= !lit;
         }
     }
-    float lit_sum = 0.0f, total = 0.0f;
+    Acc lit_sum, total;
     for (uint32_t taken = 0; taken < s.samples; ++taken) {
         if (taken == s.minimum && any_lit != any_blocked) break;
         float w;
         bool unblocked;
         if (trace(spread_point(taken), w, unblocked)) {
-            total += w;
-            lit_sum += unblocked ? w : 0.0f;
+            total.add(w);
+            lit_sum.add(unblocked ? w : 0.0f);
             any_lit |= unblocked;
             any_blocked |= !unblocked;
         }
     }
     if (any_lit != any_blocked) {
-        fraction = any_lit ? 1.0f : 0.0f;
+        fraction = any_lit ? 1.0 : 0.0;
         return true;
     }
-    if (total > 0.0f) {
-        fraction = lit_sum / total;
+    if (total.value() > 0.0) {
+        fraction = precision().mode == PREC_F64 ? lit_sum.d / total.d : (double)(lit_sum.s / total.s);
         return true;
     }
     return false;
@@ -234,10 +234,10 @@ inline Visibility area_visibility(const AreaShape &s, float reach, V3 pos, V3 no
     offset.x = rng.next_f32();
     offset.y = rng.next_f32();
     auto spread_point = [&](uint32_t taken) { return spread(taken, offset, s.rectangle); };
-    float fraction;
+    double fraction;
     bool some = s.rectangle ? adaptive_share(RECTANGLE_PROBES, 5, sampling, spread_point, trace, fraction)
                             : adaptive_share(TUBE_PROBES, 3, sampling, spread_point, trace, fraction);
-    return {some, some ? fraction : 0.0f, rays};
+    return {some, some ? fraction : 0.0, rays};
 }
 
 // sun_visibility (sun.rs:21-56). `occluded(dir)` traces to infinity.
@@ -265,9 +265,9 @@ inline Visibility sun_visibility(V3 toward, float radius, float tan_radius, V3 n
     offset.x = rng.next_f32();
     offset.y = rng.next_f32();
     auto spread_point = [&](uint32_t taken) { return concentric_disk(spread(taken, offset, true)); };
-    float fraction;
+    double fraction;
     bool some = adaptive_share(DISK_PROBES, 5, sampling, spread_point, trace, fraction);
-    return {some, some ? fraction : 0.0f, rays};
+    return {some, some ? fraction : 0.0, rays};
 }
 
 // sky_visibility (sky.rs:30-44)
@@ -279,7 +279,9 @@ inline Visibility sky_visibility(V3 normal, uint32_t samples, Rng &rng, Occ occl
     uint32_t open = 0;
     for (uint32_t taken = 0; taken < samples; ++taken)
         if (!occluded(cosine_direction(normal, spread(taken, offset, true)))) ++open;
-    return {true, (float)open / (float)std::max(samples, 1u), samples};
+    double fraction = precision().mode == PREC_F64 ? (double)open / (double)std::max(samples, 1u)
+                                                   : (double)((float)open / (float)std::max(samples, 1u));
+    return {true, fraction, samples};
 }
 
 // is_buried (mesh_texels.rs:111-135)

@@ -267,4 +267,65 @@ inline V3 on_unit_sphere(Rng &rng) {
     return V3{r * c, r * s, z};
 }
 
+// ---- precision modes ------------------------------------------------------------------------
+// F32 restates the reference's binary32 arithmetic. REFINED restates the GPU library's refined
+// form: binary32, except that ray/triangle tests landing within eps of a boundary are re-run
+// in binary64 and soft-visibility weights and bounce gathers use Kahan sums. F64 is the FP64
+// oracle: every ray/triangle test, the soft-visibility and bounce sums and the fractions they
+// give in binary64, over the same binary32 samples (origins, directions, weights, integrands),
+// so it measures the predicates and the accumulation, not the sampling.
+enum Precision : uint32_t { PREC_F32 = 0, PREC_REFINED = 1, PREC_F64 = 2 };
+struct PrecisionMode {
+    Precision mode = PREC_F32;
+    float eps = 1.0e-5f, eps2 = 1.0e-10f;
+};
+inline PrecisionMode &precision() {
+    static PrecisionMode p;
+    return p;
+}
+
+struct D3 {
+    double x, y, z;
+};
+inline D3 widen(V3 a) { return D3{(double)a.x, (double)a.y, (double)a.z}; }
+inline D3 operator-(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline double dot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline D3 cross(D3 a, D3 b) { return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
+
+// A running sum of binary32 terms in the active mode: plain binary32, Kahan (REFINED) or
+// binary64 (F64).
+struct Acc {
+    float s = 0.0f, c = 0.0f;
+    double d = 0.0;
+    void add(float x) {
+        switch (precision().mode) {
+        case PREC_F64: d += (double)x; break;
+        case PREC_REFINED: {
+            float y = x - c;
+            float t = s + y;
+            c = (t - s) - y;
+            s = t;
+            break;
+        }
+        default: s = s + x;
+        }
+    }
+    double value() const { return precision().mode == PREC_F64 ? d : (double)s; }
+};
+struct Acc3 {
+    Acc x, y, z;
+    void add(V3 v) {
+        x.add(v.x);
+        y.add(v.y);
+        z.add(v.z);
+    }
+    // sum * scale / n: binary32 in F32/REFINED (the reference's `sum * intensity / samples`),
+    // binary64 rounded once in F64
+    V3 mean(float scale, uint32_t n) const {
+        if (precision().mode == PREC_F64)
+            return V3{(float)(x.d * scale / n), (float)(y.d * scale / n), (float)(z.d * scale / n)};
+        return V3{x.s, y.s, z.s} * scale / (float)n;
+    }
+};
+
 }  // namespace oracle

@@ -91,6 +91,14 @@ inline uint8_t level(float fraction, uint32_t bits) {
     float max = (float)((1u << bits) - 1);
     return f2u8_sat(std::round(clampf(fraction, 0.0f, 1.0f) * max));
 }
+// level() of a fraction held in binary64: rounded in binary64 in the F64 mode, else level() of
+// the binary32 fraction
+inline uint8_t level_of(double fraction, uint32_t bits) {
+    if (precision().mode != PREC_F64) return level((float)fraction, bits);
+    double max = (double)((1u << bits) - 1);
+    double v = std::round(std::min(std::max(fraction, 0.0), 1.0) * max);
+    return (uint8_t)v;
+}
 struct ShadowGrid {
     uint32_t width = 0, height = 0, bits = 1;
     std::vector<uint8_t> levels;  // one per texel; packed on output
@@ -409,7 +417,7 @@ struct OccluderTriangle {
 };
 
 // intersect (occluder.rs:225-251): two-sided Möller–Trumbore, hits with 0 <= t <= max.
-inline bool intersect(const V3 v[3], V3 o, V3 d, float max, float &t_out, V3 &w_out) {
+inline bool intersect_f32(const V3 v[3], V3 o, V3 d, float max, float &t_out, V3 &w_out) {
     V3 e1 = v[1] - v[0];
     V3 e2 = v[2] - v[0];
     V3 p = cross(d, e2);
@@ -429,6 +437,74 @@ inline bool intersect(const V3 v[3], V3 o, V3 d, float max, float &t_out, V3 &w_
         return true;
     }
     return false;
+}
+
+// The same test in binary64 on the widened vertices and ray; t, u, v are rounded to binary32
+// once and w = (1 - u - v, u, v) is formed from the rounded u, v in binary32.
+inline bool intersect_f64(const V3 v[3], V3 o, V3 d, float max, float &t_out, V3 &w_out) {
+    D3 a = widen(v[0]);
+    D3 e1 = widen(v[1]) - a, e2 = widen(v[2]) - a;
+    D3 dd = widen(d);
+    D3 p = cross(dd, e2);
+    double det = dot(e1, p);
+    if (det == 0.0 || !std::isfinite(det)) return false;
+    double inv = 1.0 / det;
+    D3 s = widen(o) - a;
+    double u = dot(s, p) * inv;
+    if (!(u >= 0.0 && u <= 1.0)) return false;
+    D3 q = cross(s, e1);
+    double vv = dot(dd, q) * inv;
+    if (vv < 0.0 || u + vv > 1.0) return false;
+    double t = dot(e2, q) * inv;
+    if (!(t >= 0.0 && t <= (double)max)) return false;
+    float uf = (float)u, vf = (float)vv;
+    t_out = (float)t;
+    w_out = V3{1.0f - uf - vf, uf, vf};
+    return true;
+}
+
+inline std::atomic<uint64_t> &retest_count() {
+    static std::atomic<uint64_t> n{0};
+    return n;
+}
+
+// The refined form's test: binary32 decides unless the ray is nearly parallel to the plane
+// (det^2 <= eps^2 |e1|^2 |d x e2|^2) or u, v, u + v or t lie within eps of their bounds (t's
+// margin eps * max(1, max) for a finite max, else eps); then intersect_f64 decides.
+inline bool intersect_refined(const V3 v[3], V3 o, V3 d, float max, float &t_out, V3 &w_out) {
+    const float eps = precision().eps;
+    V3 e1 = v[1] - v[0];
+    V3 e2 = v[2] - v[0];
+    V3 p = cross(d, e2);
+    float det = dot(e1, p);
+    if (det * det > precision().eps2 * (dot(e1, e1) * dot(p, p))) {
+        float inv = 1.0f / det;
+        V3 s = o - v[0];
+        float u = dot(s, p) * inv;
+        if (!(u >= -eps && u <= 1.0f + eps)) return false;
+        V3 q = cross(s, e1);
+        float vv = dot(d, q) * inv;
+        if (!(vv >= -eps) || u + vv > 1.0f + eps) return false;
+        float t = dot(e2, q) * inv;
+        float margin = eps * (std::isfinite(max) ? fmax_r(max, 1.0f) : 1.0f);
+        if (!(t >= -margin && t <= max + margin)) return false;
+        bool near = u < eps || u > 1.0f - eps || vv < eps || u + vv > 1.0f - eps || t < margin || t > max - margin;
+        if (!near) {
+            t_out = t;
+            w_out = V3{1.0f - u - vv, u, vv};
+            return true;
+        }
+    }
+    retest_count().fetch_add(1, std::memory_order_relaxed);
+    return intersect_f64(v, o, d, max, t_out, w_out);
+}
+
+inline bool intersect(const V3 v[3], V3 o, V3 d, float max, float &t_out, V3 &w_out) {
+    switch (precision().mode) {
+    case PREC_F64: return intersect_f64(v, o, d, max, t_out, w_out);
+    case PREC_REFINED: return intersect_refined(v, o, d, max, t_out, w_out);
+    default: return intersect_f32(v, o, d, max, t_out, w_out);
+    }
 }
 
 // AlphaTexture::is_opaque (input.rs:79-97)
@@ -608,6 +684,7 @@ struct Occluders {
         bool found = false;
         float best = 0;
         uint32_t best_i = 0;
+        V3 best_w{0, 0, 0};
         auto consider = [&](uint32_t i) {
             float t;
             V3 w;
@@ -616,6 +693,7 @@ struct Occluders {
                 found = true;
                 best = t;
                 best_i = i;
+                best_w = w;
             }
         };
         if (brute_force) {
@@ -640,6 +718,12 @@ struct Occluders {
             }
         }
         if (!found) return false;
+        if (precision().mode != PREC_F32) {
+            // the winning test's own barycentrics (a re-test with max = infinity could take the
+            // other precision path)
+            out = SurfaceHit{best, best_i, best_w};
+            return true;
+        }
         float t;
         V3 w;
         if (!intersect(triangles[best_i].v, o, d, INFINITY, t, w)) return false;
