@@ -191,8 +191,11 @@ def main():
 
     # device-resident: one session, repeated runs
     session = dl.Session(inp, opts, form="batched", device=local)
+    tune = None
     for _ in range(args.warmup):
         session.run()
+        if tune is None:
+            tune = session.report()  # the first run times candidate launch shapes (then cached)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -278,6 +281,11 @@ def main():
                    "plain_form_ms": plain_rep.ms_device, "plain_visibility_ms": plain_rep.ms_visibility,
                    "batched_visibility_ms": vis,
                    "speedup_batched_vs_plain": plain_rep.ms_device / ms if ms else None,
+                   "launch_shape": {"chunk_texels": rep.tuned_chunk_texels, "sample_lanes": rep.tuned_sample_lanes,
+                                    "blocks_per_sm": rep.tuned_blocks_per_sm,
+                                    "stack_depth": rep.tuned_stack_depth, "launch_bound_blocks": rep.tuned_min_blocks,
+                                    "autotune_trials": tune.tune_trials if tune else 0,
+                                    "autotune_ms": tune.ms_tune if tune else 0.0},
                    "parallelism": f"replicas x{world}"},
         "clocks": clocks.summary(),
         "gpu_launches": int(rep.kernel_launches),

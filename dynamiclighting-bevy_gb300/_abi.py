@@ -55,7 +55,8 @@ class DlBakeConfig(C.Structure):
     _fields_ = [("form", C.c_uint32), ("device", C.c_uint32), ("block_threads", C.c_uint32),
                 ("chunk_texels", C.c_uint32), ("sample_lanes", C.c_uint32),
                 ("blocks_per_sm", C.c_uint32), ("count_visits", C.c_uint32),
-                ("refine_epsilon", C.c_float), ("reserved", C.c_uint32 * 6)]
+                ("refine_epsilon", C.c_float), ("no_autotune", C.c_uint32),
+                ("reserved", C.c_uint32 * 5)]
 
 
 class DlBakeReport(C.Structure):
@@ -68,7 +69,10 @@ class DlBakeReport(C.Structure):
                 ("d2h_bytes", C.c_uint64), ("device_bytes", C.c_uint64),
                 ("node_visits", C.c_uint64), ("tri_tests", C.c_uint64),
                 ("ms_stages", C.c_double * 8), ("ms_host", C.c_double * 4),
-                ("retests", C.c_uint64)]
+                ("retests", C.c_uint64), ("tuned_chunk_texels", C.c_uint32),
+                ("tuned_sample_lanes", C.c_uint32), ("tuned_blocks_per_sm", C.c_uint32),
+                ("tuned_stack_depth", C.c_uint32), ("tuned_min_blocks", C.c_uint32),
+                ("tune_trials", C.c_uint32), ("ms_tune", C.c_double)]
 
 
 class DlLightBvhNode(C.Structure):

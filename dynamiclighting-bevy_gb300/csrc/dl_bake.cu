@@ -26,6 +26,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "dl_kernels.cuh"
@@ -288,14 +289,46 @@ struct TraceArgs {
     const uint32_t *region_rect, *region_off;
     uint32_t *region_pool;
     Counters *ctr;
-    // batched queue
+    // batched queue: items of sky pairs first, then soft, then hard
     const uint32_t *order, *item_off;
     uint32_t pairs;
     unsigned long long items;
-    unsigned long long *head;
+    unsigned long long *head;      // chunks claimed in the per-lane phase
+    unsigned long long *head_sky;  // chunks claimed in the grouped sky phase
     const volatile uint32_t *cancel;
-    uint32_t grab;
+    uint32_t grab;         // warp-steps per claimed chunk
+    uint32_t sky_items;    // items of the sky pairs at the front of the queue
+    uint32_t sky_lanes;    // lanes sharing one sky texel's samples (1: no grouped phase)
+    uint32_t sample_every; // tuning trials: claim one chunk in `sample_every` (1: all)
 };
+
+// The visibility result of (pair p, texel x, y of mesh m) into the visited grid and the light's
+// region grid (mesh_bake.rs:231-248): a bit for 1-bit lights, an atomic max of the level otherwise.
+__device__ __forceinline__ void store_texel(const DevScene &sc, const TraceArgs &a, uint32_t m, uint32_t s,
+                                            uint32_t x, uint32_t y, uint32_t level, uint32_t bits) {
+    uint32_t res = sc.mesh_res[m];
+    uint64_t bit = (uint64_t)x + (uint64_t)y * res;
+    atomicOr(a.visited + a.grid_off[m] + bit / 32, 1u << (bit % 32));
+    size_t e = (size_t)m * sc.light_count + s;
+    const uint32_t *r = a.region_rect + e * 4;
+    uint32_t w = r[2] - r[0] + 1;
+    uint64_t idx = (uint64_t)(x - r[0]) + (uint64_t)(y - r[1]) * w;
+    uint32_t *g = a.region_pool + a.region_off[e];
+    if (bits == 1) {
+        if (level) atomicOr(g + idx / 32, 1u << (idx % 32));
+    } else if (level) {
+        uint32_t *word = g + idx / 4;
+        uint32_t shift = (uint32_t)(idx % 4) * 8;
+        uint32_t cur = *word;
+        for (;;) {
+            if (((cur >> shift) & 0xFFu) >= level) break;
+            uint32_t want = (cur & ~(0xFFu << shift)) | (level << shift);
+            uint32_t prev = atomicCAS(word, cur, want);
+            if (prev == cur) break;
+            cur = prev;
+        }
+    }
+}
 
 // One (pair, texel) of the visibility loop (mesh_bake.rs:231-248); returns the rays traced.
 template <bool COUNT = false, bool REFINE = false>
@@ -313,57 +346,104 @@ __device__ __forceinline__ uint32_t trace_texel(const DevScene &sc, const TraceA
     Tracer<COUNT, REFINE> tr{sc, origin, (l.flags & kLightAlpha) != 0, stack, stride, vis};
     Vis v = texel_shadow(sc, s, sc.mesh_id[m], x, y, pos, nrm, tr);
     if (!v.some) return 0;
-    uint32_t res = sc.mesh_res[m];
-    uint64_t bit = (uint64_t)x + (uint64_t)y * res;
-    atomicOr(a.visited + a.grid_off[m] + bit / 32, 1u << (bit % 32));
-    size_t e = (size_t)m * sc.light_count + s;
-    const uint32_t *r = a.region_rect + e * 4;
-    uint32_t w = r[2] - r[0] + 1;
-    uint64_t idx = (uint64_t)(x - r[0]) + (uint64_t)(y - r[1]) * w;
-    uint32_t *g = a.region_pool + a.region_off[e];
-    if (l.shadow_bits == 1) {
-        if (v.level) atomicOr(g + idx / 32, 1u << (idx % 32));
-    } else if (v.level) {
-        uint32_t *word = g + idx / 4;
-        uint32_t shift = (uint32_t)(idx % 4) * 8;
-        uint32_t cur = *word;
-        for (;;) {
-            if (((cur >> shift) & 0xFFu) >= v.level) break;
-            uint32_t want = (cur & ~(0xFFu << shift)) | (v.level << shift);
-            uint32_t prev = atomicCAS(word, cur, want);
-            if (prev == cur) break;
-            cur = prev;
-        }
-    }
+    store_texel(sc, a, m, s, x, y, v.level, l.shadow_bits);
     return v.rays;
 }
 
+// The pair holding queue item `item`: item_off[lo] <= item < item_off[lo + 1].
+__device__ __forceinline__ uint32_t pair_of(const TraceArgs &a, unsigned long long item) {
+    uint32_t lo = 0, hi = a.pairs;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if ((unsigned long long)a.item_off[mid] <= item) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Claims the next chunk of a queue phase for the warp: the first item of chunk c is
+// first + c * size * sample_every. Returns `end` when the phase is drained or cancelled.
+__device__ __forceinline__ unsigned long long claim(const TraceArgs &a, unsigned long long *head,
+                                                    unsigned long long first, unsigned long long size,
+                                                    unsigned long long end, uint32_t &grabs) {
+    unsigned long long base = 0;
+    if (lane_id() == 0) {
+        unsigned long long c = atomicAdd(head, 1ull);
+        base = first + c * size * a.sample_every;
+        if ((++grabs & 15u) == 0 && *a.cancel) base = end;
+        if (base > end) base = end;
+    }
+    return __shfl_sync(0xFFFFFFFFu, base, 0);
+}
+
 // Batched form: persistent warps pull chunks of (pair, texel) items from one queue. Items are
-// ordered sky pairs first, then soft, then hard, so the longest work starts first.
-template <bool COUNT, bool REFINE>
-__global__ void __launch_bounds__(kBlock, 7) k_trace_batched(DevScene sc, TraceArgs a) {
-    __shared__ int stack[kStack * kBlock];
+// ordered sky pairs first, then soft, then hard, so the longest work starts first. With
+// sky_lanes = W > 1 the sky items run first in a grouped phase: W lanes share one texel, each
+// tracing every W-th of its samples, and the open counts are summed across the group (an integer
+// sum, so the level is the same as one lane tracing them all in order). MINB is the launch bound's
+// blocks per SM (the register budget). The stack lives in dynamic shared memory.
+template <bool COUNT, bool REFINE, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) k_trace_batched(DevScene sc, TraceArgs a) {
+    extern __shared__ int stack[];
     int *my = stack + threadIdx.x;
     unsigned lane = lane_id();
     unsigned long long rays = 0;
     Visits vis{0, 0, 0};
     uint32_t grabs = 0;
+    const uint32_t W = a.sky_lanes;
+    unsigned long long first = 0;
+    if (W > 1 && a.sky_items) {
+        const uint32_t per_step = 32 / W, sub = lane % W;
+        const unsigned long long end = a.sky_items;
+        first = end;
+        for (;;) {
+            unsigned long long base = claim(a, a.head_sky, 0, (unsigned long long)per_step * a.grab, end, grabs);
+            if (base >= end) break;
+            uint32_t cur = pair_of(a, base);
+            for (uint32_t g = 0; g < a.grab; ++g) {
+                unsigned long long item = base + (unsigned long long)g * per_step + lane / W;
+                bool valid = item < end;
+                uint32_t open = 0, t = 0, s = 0, m = 0, x = 0, y = 0;
+                if (valid) {
+                    while ((unsigned long long)a.item_off[cur + 1] <= item) ++cur;
+                    uint32_t p = a.order[cur];
+                    t = a.pair_tri[p];
+                    s = a.pair_light[p];
+                    m = sc.tri_mesh[t];
+                    uint32_t ci = a.ctex_off[t] + (uint32_t)(item - a.item_off[cur]);
+                    uint32_t xy = a.ctex_xy[ci];
+                    x = xy & 0xFFFFu;
+                    y = xy >> 16;
+                    float4 pp = a.ctex_pos[ci], nn = a.ctex_nrm[ci], f = a.tri_face[t];
+                    f3 nrm{nn.x, nn.y, nn.z};
+                    f3 origin = add(f3{pp.x, pp.y, pp.z}, scale(f3{f.x, f.y, f.z}, kRayOffset));
+                    const DevLight &l = sc.lights[s];
+                    Tracer<COUNT, REFINE> tr{sc, origin, (l.flags & kLightAlpha) != 0, my, kBlock, &vis};
+                    // sky_visibility (sky.rs:30-44), samples sub, sub + W, ...
+                    Pcg rng = stream5(sc.seed, sc.mesh_id[m], l.id, x, y);
+                    f2 off;
+                    off.x = rng.next_f32();
+                    off.y = rng.next_f32();
+                    f3 side, across;
+                    ortho_pair(nrm, side, across);
+                    for (uint32_t j = sub; j < sc.sky_samples; j += W)
+                        if (!tr(cosine_direction_basis(nrm, side, across, spread(j, off, true)), INFINITY)) ++open;
+                }
+                for (uint32_t o = 1; o < W; o <<= 1) open += __shfl_xor_sync(0xFFFFFFFFu, open, o);
+                if (valid && sub == 0) {
+                    uint32_t samples = sc.sky_samples;
+                    float fraction = (float)open / (float)(samples > 1 ? samples : 1);
+                    const DevLight &l = sc.lights[s];
+                    store_texel(sc, a, m, s, x, y, level_of(fraction, l.shadow_bits), l.shadow_bits);
+                    rays += samples;
+                }
+            }
+        }
+    }
     for (;;) {
-        unsigned long long base = 0;
-        if (lane == 0) {
-            base = atomicAdd(a.head, (unsigned long long)(32 * a.grab));
-            if ((++grabs & 15u) == 0 && *a.cancel) base = a.items;
-        }
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        unsigned long long base = claim(a, a.head, first, 32ull * a.grab, a.items, grabs);
         if (base >= a.items) break;
-        // the chunk's first pair: item_off[lo] <= base < item_off[lo + 1]
-        uint32_t lo = 0, hi = a.pairs;
-        while (hi - lo > 1) {
-            uint32_t mid = (lo + hi) >> 1;
-            if ((unsigned long long)a.item_off[mid] <= base) lo = mid;
-            else hi = mid;
-        }
-        uint32_t cur = lo;  // per lane, advances monotonically over the chunk
+        uint32_t cur = pair_of(a, base);  // per lane, advances monotonically over the chunk
         for (uint32_t g = 0; g < a.grab; ++g) {
             unsigned long long item = base + (unsigned long long)g * 32 + lane;
             if (item < a.items) {
@@ -1129,6 +1209,7 @@ struct dl_session {
     uint64_t graph_generation = ~0ull;
     unsigned long long graph_items = 0;
     unsigned graph_blocks = 0;
+    uint64_t graph_shape = 0;
     ~dl_session() {
         if (graph) cudaGraphExecDestroy(graph);
         for (auto &e : marks)
@@ -1187,6 +1268,11 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     if (cfg) s->config = *cfg;
     if (s->config.form > DL_FORM_REFINED) {
         g_error = "unknown bake form " + std::to_string(s->config.form);
+        return DL_INVALID_ARGUMENT;
+    }
+    uint32_t lanes = s->config.sample_lanes;
+    if (lanes > 32 || (lanes & (lanes - 1))) {
+        g_error = "sample_lanes must be 0 or a power of two up to 32";
         return DL_INVALID_ARGUMENT;
     }
     float eps = s->config.refine_epsilon;
@@ -1338,6 +1424,120 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
 
 // The device pipeline of one bake. Reads back the sizes it needs between stages; everything
 // else stays on the device until dl_session_result.
+// ---- launch-shape autotuner of the batched visibility kernel ---------------------------------
+// Knobs: chunk size (warp-steps per claimed chunk), sky sample lanes (lanes sharing one sky
+// texel), the launch bound's blocks per SM (register budget 72 or 64 per thread) and the stack
+// depth (the BVH's depth, rounded up; it sets the shared memory per block and so, with the
+// registers, the resident blocks). Each candidate runs on every k-th chunk of the real queue
+// (k = 8 from 4 M items, 4 from 1 M) with scratch counters; its results are the same levels the
+// real pass writes (OR and max), so the trials change no output. The fastest shape is cached per
+// process, keyed by the device and the queue's shape.
+struct TraceTune {
+    uint32_t grab = 1, sky_lanes = 1, minb = 7, stack_depth = kStack, blocks = 1, trials = 0;
+    double ms = 0.0;
+};
+using TraceKernel = void (*)(DevScene, TraceArgs);
+
+TraceKernel trace_kernel(bool count, bool refine, uint32_t minb) {
+    if (count) return refine ? k_trace_batched<true, true, 7> : k_trace_batched<true, false, 7>;
+    if (refine) return k_trace_batched<false, true, 7>;
+    return minb == 8 ? k_trace_batched<false, false, 8> : k_trace_batched<false, false, 7>;
+}
+
+struct TuneKey {
+    int device;
+    uint64_t items, sky_items, pairs, occluders, nodes;
+    uint32_t depth, flags, fixed;
+    bool operator<(const TuneKey &o) const {
+        return std::tie(device, items, sky_items, pairs, occluders, nodes, depth, flags, fixed) <
+               std::tie(o.device, o.items, o.sky_items, o.pairs, o.occluders, o.nodes, o.depth, o.flags, o.fixed);
+    }
+};
+std::mutex g_tune_lock;
+std::map<TuneKey, TraceTune> g_tune_cache;
+
+TraceTune trace_tune(dl_session &s, TraceArgs ta, bool refine, bool count, dl_progress *progress) {
+    const dl_bake_config &c = s.config;
+    TraceTune best;
+    best.stack_depth = std::max<uint32_t>(8, (s.host.bvh_depth + 3) & ~3u);
+    auto blocks_for = [&](uint32_t minb) {
+        int per_sm = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel(count, refine, minb), kBlock,
+                                                         (size_t)best.stack_depth * kBlock * sizeof(int)));
+        if (c.blocks_per_sm) per_sm = std::min(per_sm, (int)c.blocks_per_sm);
+        return (uint32_t)std::max(1, per_sm) * (uint32_t)s.sms;
+    };
+    std::vector<uint32_t> grabs = c.chunk_texels ? std::vector<uint32_t>{std::max(1u, c.chunk_texels / 32)}
+                                                 : std::vector<uint32_t>{1, 2};
+    std::vector<uint32_t> lanes = c.sample_lanes ? std::vector<uint32_t>{c.sample_lanes}
+                                  : ta.sky_items  ? std::vector<uint32_t>{1, 4, 8}
+                                                  : std::vector<uint32_t>{1};
+    std::vector<uint32_t> minbs = (count || refine) ? std::vector<uint32_t>{7} : std::vector<uint32_t>{7, 8};
+    const uint32_t every = ta.items >= (4u << 20) ? 8 : ta.items >= (1u << 20) ? 4 : 0;
+    const bool tune = !c.no_autotune && every && grabs.size() * lanes.size() * minbs.size() > 1 &&
+                      !(progress && progress->cancel);
+    best.grab = grabs[0];
+    best.sky_lanes = lanes[0];
+    best.minb = minbs[0];
+    if (!tune) {
+        best.blocks = blocks_for(best.minb);
+        return best;
+    }
+    TuneKey key{s.device, ta.items, ta.sky_items, ta.pairs, s.host.tri_v0.size(), s.host.nodes.size(),
+                best.stack_depth, (count ? 1u : 0u) | (refine ? 2u : 0u),
+                c.chunk_texels | (c.sample_lanes << 16) | (c.blocks_per_sm << 24)};
+    {
+        std::lock_guard<std::mutex> guard(g_tune_lock);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            TraceTune hit = it->second;
+            hit.trials = 0;
+            hit.ms = 0.0;
+            return hit;
+        }
+    }
+    cudaStream_t st = s.stream;
+    Counters *scratch = s.pool.get<Counters>("tune_counters", 1);
+    ta.ctr = scratch;
+    ta.sample_every = every;
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    float best_ms = INFINITY;
+    auto t0 = std::chrono::steady_clock::now();
+    for (uint32_t minb : minbs) {
+        uint32_t blocks = blocks_for(minb);
+        for (uint32_t w : lanes)
+            for (uint32_t g : grabs) {
+                ta.grab = g;
+                ta.sky_lanes = w;
+                CK(cudaMemsetAsync(ta.head, 0, 2 * sizeof(unsigned long long), st));
+                CK(cudaEventRecord(a, st));
+                trace_kernel(count, refine, minb)<<<blocks, kBlock, (size_t)best.stack_depth * kBlock * sizeof(int),
+                                                     st>>>(s.sc, ta);
+                CK(cudaGetLastError());
+                CK(cudaEventRecord(b, st));
+                CK(cudaEventSynchronize(b));
+                float ms = 0.0f;
+                CK(cudaEventElapsedTime(&ms, a, b));
+                ++best.trials;
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best.grab = g;
+                    best.sky_lanes = w;
+                    best.minb = minb;
+                    best.blocks = blocks;
+                }
+            }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    best.ms = ms_since(t0);
+    std::lock_guard<std::mutex> guard(g_tune_lock);
+    g_tune_cache[key] = best;
+    return best;
+}
+
 dl_status run(dl_session &s, dl_progress *progress) {
     DevScene &sc = s.sc;
     const uint32_t T = sc.triangles, M = sc.mesh_count, L = sc.light_count;
@@ -1371,6 +1571,9 @@ dl_status run(dl_session &s, dl_progress *progress) {
     CK(cudaMemsetAsync(s.ctr, 0, sizeof(Counters), st));
     CK(cudaMemsetAsync(s.cancel_dev, 0, 4, st));
     s.report.photon_rays = 0;
+    s.report.tuned_chunk_texels = s.report.tuned_sample_lanes = s.report.tuned_blocks_per_sm = 0;
+    s.report.tuned_stack_depth = s.report.tuned_min_blocks = s.report.tune_trials = 0;
+    s.report.ms_tune = 0.0;
     if (T == 0) {
         // no triangles: every mesh serializes to no words (triangle_words.rs:47-56)
         CK(cudaEventRecord(v0, st));
@@ -1532,7 +1735,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
         uint32_t *order = P.get<uint32_t>("order", pairs + 1);
         uint32_t *flag = P.get<uint32_t>("flag", pairs + 1);
         uint32_t *fpos = P.get<uint32_t>("fpos", pairs + 1);
-        uint32_t base = 0;
+        uint32_t base = 0, sky_pairs = 0;
         for (uint32_t c = 0; c < 3; ++c) {
             k_pair_class<<<grid_for(pairs + 1), kBlock, 0, st>>>(sc, pair_light, pairs, c, flag);
             LAUNCHED("k_pair_class");
@@ -1541,6 +1744,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
             LAUNCHED("k_pair_scatter");
             s.launches += 2;
             base += read_back(s, fpos + pairs);
+            if (c == 0) sky_pairs = base;
         }
         uint32_t *icnt = P.get<uint32_t>("icnt", pairs + 1);
         uint32_t *item_off = P.get<uint32_t>("item_off", pairs + 1);
@@ -1549,36 +1753,51 @@ dl_status run(dl_session &s, dl_progress *progress) {
         ++s.launches;
         scan_u32(s, icnt, item_off, pairs + 1);
         const uint32_t items = read_back(s, item_off + pairs);
+        const uint32_t sky_items = sky_pairs ? read_back(s, item_off + sky_pairs) : 0;
         s.report.work_items = items;
-        unsigned long long *head = P.get<unsigned long long>("head", 1);
+        unsigned long long *heads = P.get<unsigned long long>("heads", 2);
         ta.order = order;
         ta.item_off = item_off;
         ta.pairs = pairs;
         ta.items = items;
-        ta.head = head;
-        ta.grab = s.config.chunk_texels ? std::max(1u, s.config.chunk_texels / 32) : 1;
-        int per_sm = 0;
+        ta.head = heads;
+        ta.head_sky = heads + 1;
+        ta.sky_items = sky_items;
+        ta.sample_every = 1;
         const bool count = s.config.count_visits != 0;  // instrumented variant: counts node visits
-        auto trace = refine ? (count ? k_trace_batched<true, true> : k_trace_batched<false, true>)
-                            : (count ? k_trace_batched<true, false> : k_trace_batched<false, false>);
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace, kBlock, 0));
-        if (s.config.blocks_per_sm) per_sm = std::min(per_sm, (int)s.config.blocks_per_sm);
-        unsigned blocks = (unsigned)std::max(1, per_sm * s.sms);
-        // The visibility stage runs from a CUDA graph: the memset of the queue head and the
-        // persistent kernel, captured once per queue layout and replayed.
-        if (!s.graph || s.graph_generation != P.generation || s.graph_items != items || s.graph_blocks != blocks) {
+        TraceTune tune = trace_tune(s, ta, refine, count, progress);
+        s.report.tuned_chunk_texels = tune.grab * 32;
+        s.report.tuned_sample_lanes = tune.sky_lanes;
+        s.report.tuned_blocks_per_sm = tune.blocks / (uint32_t)s.sms;
+        s.report.tuned_stack_depth = tune.stack_depth;
+        s.report.tuned_min_blocks = tune.minb;
+        s.report.tune_trials = tune.trials;
+        s.report.ms_tune = tune.ms;
+        ta.grab = tune.grab;
+        ta.sky_lanes = tune.sky_lanes;
+        auto trace = trace_kernel(count, refine, tune.minb);
+        const size_t smem = (size_t)tune.stack_depth * kBlock * sizeof(int);
+        const unsigned blocks = tune.blocks;
+        // The visibility stage runs from a CUDA graph: the memset of the queue heads and the
+        // persistent kernel, captured once per queue layout and launch shape and replayed.
+        const uint64_t shape = ((uint64_t)tune.grab << 40) ^ ((uint64_t)tune.sky_lanes << 32) ^
+                               ((uint64_t)tune.minb << 24) ^ ((uint64_t)tune.stack_depth << 16) ^ (count ? 1 : 0) ^
+                               (refine ? 2 : 0);
+        if (!s.graph || s.graph_generation != P.generation || s.graph_items != items || s.graph_blocks != blocks ||
+            s.graph_shape != shape) {
             if (s.graph) cudaGraphExecDestroy(s.graph);
             s.graph = nullptr;
             cudaGraph_t g;
             CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            cudaMemsetAsync(head, 0, sizeof(unsigned long long), st);
-            if (items) trace<<<blocks, kBlock, 0, st>>>(sc, ta);
+            cudaMemsetAsync(heads, 0, 2 * sizeof(unsigned long long), st);
+            if (items) trace<<<blocks, kBlock, smem, st>>>(sc, ta);
             CK(cudaStreamEndCapture(st, &g));
             CK(cudaGraphInstantiate(&s.graph, g, 0));
             cudaGraphDestroy(g);
             s.graph_generation = P.generation;
             s.graph_items = items;
             s.graph_blocks = blocks;
+            s.graph_shape = shape;
         }
         CK(cudaEventRecord(v0, st));
         CK(cudaGraphLaunch(s.graph, st));

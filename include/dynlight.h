@@ -154,14 +154,17 @@ typedef struct dl_bake_config {
     uint32_t form;             /* DL_FORM_* */
     uint32_t device;           /* CUDA device ordinal */
     uint32_t block_threads;    /* 0: tuned default */
-    uint32_t chunk_texels;     /* texels per work item of the batched queue, 0: default */
-    uint32_t sample_lanes;     /* lanes sharing one texel's soft/sky samples, 0: default */
-    uint32_t blocks_per_sm;    /* persistent blocks per SM, 0: default */
+    uint32_t chunk_texels;     /* (pair, texel) items a warp claims from the queue at once, 0: tuned */
+    uint32_t sample_lanes;     /* lanes sharing one sky texel's samples (1, 2, 4, 8, 16 or 32), 0: tuned */
+    uint32_t blocks_per_sm;    /* upper bound of persistent blocks per SM, 0: as many as fit */
     uint32_t count_visits;     /* 1: run the instrumented visibility kernel that counts BVH node
                                   visits and triangle tests (for roofline accounting; slower) */
     float refine_epsilon;      /* DL_FORM_REFINED: re-test margin (barycentric units; times
                                   max(1, ray length) for distances), 0: 1e-5 */
-    uint32_t reserved[6];
+    uint32_t no_autotune;      /* 1: never time candidate launch shapes; unset knobs take defaults.
+                                  0: knobs left 0 are picked by timing trials on the first run of a
+                                  scene shape (cached per process) */
+    uint32_t reserved[5];
 } dl_bake_config;
 
 /* Timings (device events, milliseconds) and counters of the last bake. */
@@ -191,6 +194,11 @@ typedef struct dl_bake_report {
     double ms_host[4];        /* host time of session creation: validation + sorting + lights,
                                  occluder BVH build, flattening + uploads, unused */
     uint64_t retests;         /* DL_FORM_REFINED: ray/triangle tests re-run in binary64 */
+    /* launch shape of the batched visibility kernel (picked by the autotuner or the config) */
+    uint32_t tuned_chunk_texels, tuned_sample_lanes, tuned_blocks_per_sm, tuned_stack_depth;
+    uint32_t tuned_min_blocks;  /* launch bound: blocks per SM the registers were sized for */
+    uint32_t tune_trials;       /* candidate shapes timed in this run (0: defaults or cached) */
+    double ms_tune;             /* host time of those trials */
 } dl_bake_report;
 
 /* LightBvhNode (src/bake/light_bvh.rs:16-22), 32 bytes. */

@@ -194,3 +194,35 @@ def test_tuning_does_not_change_the_bytes():
     for tuning in [dict(chunk_texels=128), dict(blocks_per_sm=1), dict(chunk_texels=32, blocks_per_sm=2)]:
         other = dl.bake(inp, opts, **tuning)
         assert other.words_equal(base) and other.stats == base.stats, tuning
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8, 32])
+def test_sky_sample_lanes_do_not_change_the_bytes(lanes):
+    # lanes sharing one sky texel's samples: an integer sum of open samples, so the same levels
+    inp, opts = fx.determinism_room()
+    want, _, _ = oracle.bake(inp, opts)
+    for chunk in (32, 96):
+        report = dl._abi.DlBakeReport()
+        got = dl.bake(inp, opts, sample_lanes=lanes, chunk_texels=chunk, report=report)
+        assert_same(got, want)
+        assert report.tuned_sample_lanes == lanes and report.tuned_chunk_texels == chunk
+
+
+def test_autotuned_launch_shape_gives_the_default_bytes():
+    # a scene with over a million queue items, so the first run times candidate shapes
+    inp, opts = scenes.outdoor(grid=193, chunks=2, boxes=150, point_lights=6, sky_samples=64, bounce_samples=16)
+    report = dl._abi.DlBakeReport()
+    tuned = dl.bake(inp, opts, report=report)
+    assert report.work_items >= (1 << 20)
+    assert report.tune_trials > 1 and report.tuned_stack_depth >= 8
+    again = dl._abi.DlBakeReport()
+    assert dl.bake(inp, opts, report=again).words_equal(tuned)
+    assert again.tune_trials == 0  # cached for this scene shape
+    assert (again.tuned_chunk_texels, again.tuned_sample_lanes) == (report.tuned_chunk_texels,
+                                                                     report.tuned_sample_lanes)
+    default = dl.bake(inp, opts, no_autotune=1)
+    assert default.words_equal(tuned) and default.stats == tuned.stats
+    fixed = dl.bake(inp, opts, sample_lanes=8, chunk_texels=64)
+    assert fixed.words_equal(tuned)
+    with pytest.raises(dl.BakeError):
+        dl.bake(inp, opts, sample_lanes=3)
