@@ -72,7 +72,8 @@ class DlBakeReport(C.Structure):
                 ("retests", C.c_uint64), ("tuned_chunk_texels", C.c_uint32),
                 ("tuned_sample_lanes", C.c_uint32), ("tuned_blocks_per_sm", C.c_uint32),
                 ("tuned_stack_depth", C.c_uint32), ("tuned_min_blocks", C.c_uint32),
-                ("tune_trials", C.c_uint32), ("ms_tune", C.c_double)]
+                ("tune_trials", C.c_uint32), ("ms_tune", C.c_double),
+                ("tuned_gather_lanes", C.c_uint32), ("reserved_report", C.c_uint32)]
 
 
 class DlLightBvhNode(C.Structure):

@@ -552,49 +552,99 @@ struct BounceArgs {
     uint32_t res;
     float4 *value;  // xyz: gathered value, w: 1 when gathered
     Counters *ctr;
+    uint32_t lanes;         // lanes sharing one texel's samples (1, 2, 4, 8, 16 or 32)
+    uint32_t sample_every;  // tuning trials: one claimed step in `sample_every` (1: all)
+    uint32_t stack_depth;   // shared-memory stack entries per thread
+    unsigned long long *head;  // steps claimed so far (32 / lanes items per step)
 };
 
-// gather_triangle / gather_sun (bounce.rs:235-292, sun_bounce.rs:24-80): one thread per
-// (bounce pair, texel).
+// gather_triangle / gather_sun (bounce.rs:235-292, sun_bounce.rs:24-80): a group of `lanes`
+// lanes per (bounce pair, texel) item. Each round, lane k of a group evaluates sample
+// round * lanes + k; the group leader then adds the round's contributions in sample order, so
+// the sum is the reference's sequential one for any group size. Dynamic shared memory holds the
+// traversal stacks and one float4 contribution slot per thread.
 template <bool REFINE>
 __global__ void __launch_bounds__(kBlock) k_gather(DevScene sc, BounceArgs a) {
-    __shared__ int stack[kStack * kBlock];
-    int *my = stack + threadIdx.x;
+    extern __shared__ int smem[];
+    int *my = smem + threadIdx.x;
+    float4 *part = reinterpret_cast<float4 *>(smem + (size_t)a.stack_depth * kBlock);
+    const uint32_t lane = lane_id(), W = a.lanes, sub = lane % W, per_step = 32 / W;
     unsigned long long rays = 0;
     Visits vis{0, 0, 0};
-    unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    for (unsigned long long item = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; item < a.items;
-         item += stride) {
-        uint32_t lo = 0, hi = a.bpair_count;
-        while (hi - lo > 1) {
-            uint32_t mid = (lo + hi) >> 1;
-            if ((unsigned long long)a.bitem_off[mid] <= item) lo = mid;
-            else hi = mid;
+    for (;;) {
+        unsigned long long step = 0;
+        if (lane == 0) step = atomicAdd(a.head, 1ull);
+        step = __shfl_sync(0xFFFFFFFFu, step, 0);
+        unsigned long long base = step * per_step * a.sample_every;
+        if (base >= a.items) break;  // uniform across the warp
+        unsigned long long item = base + lane / W;
+        bool valid = item < a.items, active = false, sun = false;
+        uint32_t samples = 0, s = 0;
+        f3 pos{0, 0, 0}, normal{0, 0, 0}, origin{0, 0, 0};
+        LocalGather lg;
+        SunGather sg;
+        if (valid) {
+            uint32_t lo = 0, hi = a.bpair_count;
+            while (hi - lo > 1) {
+                uint32_t mid = (lo + hi) >> 1;
+                if ((unsigned long long)a.bitem_off[mid] <= item) lo = mid;
+                else hi = mid;
+            }
+            uint32_t p = a.bpairs[lo];
+            uint32_t t = a.pair_tri[p];
+            s = a.pair_light[p];
+            uint32_t m = sc.tri_mesh[t];
+            uint32_t ci = a.ctex_off[t] + (uint32_t)(item - a.bitem_off[lo]);
+            uint32_t xy = a.ctex_xy[ci];
+            float4 pp = a.ctex_pos[ci], f = a.tri_face[t];
+            pos = f3{pp.x, pp.y, pp.z};
+            normal = f3{f.x, f.y, f.z};
+            origin = add(pos, scale(normal, kRayOffset));
+            const DevLight &l = sc.lights[s];
+            samples = l.bounce_samples;
+            sun = l.shape == DL_SHAPE_SUN;
+            if (sun) {
+                sun_setup(sc, l, sc.mesh_id[m], xy & 0xFFFFu, xy >> 16, normal, sg);
+                active = true;
+            } else {
+                active = local_setup(sc, l, sc.mesh_id[m], xy & 0xFFFFu, xy >> 16, pos, sub, lg);
+            }
         }
-        uint32_t p = a.bpairs[lo];
-        uint32_t t = a.pair_tri[p], s = a.pair_light[p];
-        uint32_t m = sc.tri_mesh[t];
-        uint32_t ci = a.ctex_off[t] + (uint32_t)(item - a.bitem_off[lo]);
-        uint32_t xy = a.ctex_xy[ci];
-        float4 pp = a.ctex_pos[ci], f = a.tri_face[t];
-        f3 pos{pp.x, pp.y, pp.z}, normal{f.x, f.y, f.z};
-        f3 origin = add(pos, scale(normal, kRayOffset));
-        const DevLight &l = sc.lights[s];
-        f3 v{0.0f, 0.0f, 0.0f};
-        uint32_t r = 0;
-        bool gathered = true;
-        if (l.shape == DL_SHAPE_SUN) {
-            gather_sun<REFINE>(sc, l, sc.mesh_id[m], xy & 0xFFFFu, xy >> 16, origin, normal, my, kBlock, v, r, &vis);
-        } else {
-            Tracer<false, REFINE> tr{sc, origin, (l.flags & kLightAlpha) != 0, my, kBlock, &vis};
-            gathered = gather_local(sc, l, a.photons + (size_t)l.cube * 6 * a.res * a.res, a.res, sc.mesh_id[m],
-                                    xy & 0xFFFFu, xy >> 16, pos, normal, tr, v, r);
+        if (!active) samples = 0;
+        FSum3<REFINE> sum;
+        const uint32_t rounds = __reduce_max_sync(0xFFFFFFFFu, (samples + W - 1) / W);
+        for (uint32_t r = 0; r < rounds; ++r) {
+            uint32_t i = r * W + sub;
+            Contribution c{f3{0.0f, 0.0f, 0.0f}, false, 0};
+            if (i < samples) {
+                const DevLight &l = sc.lights[s];
+                if (sun) {
+                    c = sun_sample<REFINE>(sc, l, origin, normal, sg, i, my, kBlock, &vis);
+                } else {
+                    Tracer<false, REFINE> tr{sc, origin, (l.flags & kLightAlpha) != 0, my, kBlock, &vis};
+                    c = local_sample(sc, l, a.photons + (size_t)l.cube * 6 * a.res * a.res, a.res, normal, lg, i, tr);
+                    lg.rng.advance(2ull * (W - 1));  // to the lane's next sample, i + W
+                }
+                rays += c.rays;
+            }
+            part[threadIdx.x] = make_float4(c.value.x, c.value.y, c.value.z, c.add ? 1.0f : 0.0f);
+            __syncwarp();
+            if (sub == 0 && samples) {
+                for (uint32_t k = 0; k < W && r * W + k < samples; ++k) {
+                    float4 q = part[threadIdx.x + k];
+                    if (q.w != 0.0f) sum.add(f3{q.x, q.y, q.z});
+                }
+            }
+            __syncwarp();
         }
-        rays += r;
-        a.value[item] = make_float4(v.x, v.y, v.z, gathered ? 1.0f : 0.0f);
+        if (valid && sub == 0) {
+            f3 v{0.0f, 0.0f, 0.0f};
+            if (active) v = divs(scale(sum.value(), sc.lights[s].bounce_intensity), (float)samples);
+            a.value[item] = make_float4(v.x, v.y, v.z, active ? 1.0f : 0.0f);
+        }
     }
-    unsigned long long sum = warp_sum(rays);
-    if (lane_id() == 0 && sum) atomicAdd(&a.ctr->bounce_rays, sum);
+    unsigned long long total = warp_sum(rays);
+    if (lane_id() == 0 && total) atomicAdd(&a.ctr->bounce_rays, total);
     if (REFINE) add_retests(a.ctr, vis.retests);
 }
 
@@ -1538,6 +1588,74 @@ TraceTune trace_tune(dl_session &s, TraceArgs ta, bool refine, bool count, dl_pr
     return best;
 }
 
+// The gather kernel's lanes per texel, tuned the same way (trials on every k-th step of the real
+// item list, value writes that the real pass overwrites).
+struct GatherTune {
+    uint32_t lanes = 1, stack_depth = kStack, blocks = 1, trials = 0;
+    double ms = 0.0;
+};
+size_t gather_smem(uint32_t depth) { return (size_t)depth * kBlock * sizeof(int) + kBlock * sizeof(float4); }
+std::map<TuneKey, GatherTune> g_gather_cache;
+
+GatherTune gather_tune(dl_session &s, BounceArgs ba, uint32_t bpairs, bool refine, dl_progress *progress) {
+    const dl_bake_config &c = s.config;
+    GatherTune best;
+    best.stack_depth = std::max<uint32_t>(8, (s.host.bvh_depth + 3) & ~3u);
+    auto kernel = refine ? k_gather<true> : k_gather<false>;
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, gather_smem(best.stack_depth)));
+    if (c.blocks_per_sm) per_sm = std::min(per_sm, (int)c.blocks_per_sm);
+    best.blocks = (uint32_t)std::max(1, per_sm) * (uint32_t)s.sms;
+    std::vector<uint32_t> lanes = c.sample_lanes ? std::vector<uint32_t>{c.sample_lanes}
+                                                 : std::vector<uint32_t>{1, 4, 8, 16};
+    const uint32_t every = ba.items >= (1u << 20) ? 8 : ba.items >= (1u << 18) ? 4 : 0;
+    best.lanes = lanes[0];
+    if (c.no_autotune || !every || lanes.size() == 1 || (progress && progress->cancel)) return best;
+    TuneKey key{s.device, ba.items, bpairs, 0, s.host.tri_v0.size(), s.host.nodes.size(), best.stack_depth,
+                refine ? 2u : 0u, c.blocks_per_sm};
+    {
+        std::lock_guard<std::mutex> guard(g_tune_lock);
+        auto it = g_gather_cache.find(key);
+        if (it != g_gather_cache.end()) {
+            GatherTune hit = it->second;
+            hit.trials = 0;
+            hit.ms = 0.0;
+            return hit;
+        }
+    }
+    cudaStream_t st = s.stream;
+    ba.ctr = s.pool.get<Counters>("tune_counters", 1);
+    ba.sample_every = every;
+    ba.stack_depth = best.stack_depth;
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    float best_ms = INFINITY;
+    auto t0 = std::chrono::steady_clock::now();
+    for (uint32_t w : lanes) {
+        ba.lanes = w;
+        CK(cudaMemsetAsync(ba.head, 0, sizeof(unsigned long long), st));
+        CK(cudaEventRecord(a, st));
+        kernel<<<best.blocks, kBlock, gather_smem(best.stack_depth), st>>>(s.sc, ba);
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(b, st));
+        CK(cudaEventSynchronize(b));
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, a, b));
+        ++best.trials;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best.lanes = w;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    best.ms = ms_since(t0);
+    std::lock_guard<std::mutex> guard(g_tune_lock);
+    g_gather_cache[key] = best;
+    return best;
+}
+
 dl_status run(dl_session &s, dl_progress *progress) {
     DevScene &sc = s.sc;
     const uint32_t T = sc.triangles, M = sc.mesh_count, L = sc.light_count;
@@ -1574,6 +1692,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
     s.report.tuned_chunk_texels = s.report.tuned_sample_lanes = s.report.tuned_blocks_per_sm = 0;
     s.report.tuned_stack_depth = s.report.tuned_min_blocks = s.report.tune_trials = 0;
     s.report.ms_tune = 0.0;
+    s.report.tuned_gather_lanes = 0;
     if (T == 0) {
         // no triangles: every mesh serializes to no words (triangle_words.rs:47-56)
         CK(cudaEventRecord(v0, st));
@@ -1861,11 +1980,16 @@ dl_status run(dl_session &s, dl_progress *progress) {
         ba.value = bval;
         ba.ctr = s.ctr;
         if (bitems) {
-            int per_sm = 0;
-            auto gather = refine ? k_gather<true> : k_gather<false>;
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gather, kBlock, 0));
-            unsigned blocks = (unsigned)std::min<size_t>(grid_for(bitems), (size_t)std::max(1, per_sm) * s.sms * 8);
-            gather<<<blocks, kBlock, 0, st>>>(sc, ba);
+            ba.head = P.get<unsigned long long>("gather_head", 1);
+            ba.sample_every = 1;
+            GatherTune g = gather_tune(s, ba, bcount, refine, progress);
+            ba.lanes = g.lanes;
+            ba.stack_depth = g.stack_depth;
+            s.report.tuned_gather_lanes = g.lanes;
+            s.report.tune_trials += g.trials;
+            s.report.ms_tune += g.ms;
+            CK(cudaMemsetAsync(ba.head, 0, sizeof(unsigned long long), st));
+            (refine ? k_gather<true> : k_gather<false>)<<<g.blocks, kBlock, gather_smem(g.stack_depth), st>>>(sc, ba);
             LAUNCHED("k_gather");
             ++s.launches;
         }

@@ -517,73 +517,95 @@ __device__ __forceinline__ f3 reflected(const DevScene &sc, f3 albedo) {
     return sc.colored_bounce ? albedo : f3{1.0f, 1.0f, 1.0f};
 }
 
-// gather_triangle's per-texel body (bounce.rs:252-289). Returns false when the texel is out of
-// the light's reach (it then gathers nothing and sets no map texel).
-template <class TR>
-__device__ __forceinline__ bool gather_local(const DevScene &sc, const DevLight &l, const Photon *cube, uint32_t res,
-                                             uint64_t mesh_id, uint32_t x, uint32_t y, f3 pos, f3 normal,
-                                             const TR &tr, f3 &value, uint32_t &rays) {
+// The gathers below split a texel's samples over a group of lanes: each lane evaluates single
+// samples and the group leader adds their contributions in sample order, so the sums are the
+// reference's sequential ones (bounce.rs:282, sun_bounce.rs:70).
+
+// One sample's contribution: `add` is false for a sample the reference skips (no sum term).
+struct Contribution {
+    f3 value;
+    bool add;
+    uint32_t rays;
+};
+
+// gather_triangle's per-texel setup (bounce.rs:252-266): false when the texel is out of reach.
+struct LocalGather {
+    f3 direction;
+    Pcg rng;  // the stream at the lane's first sample
+    float step;
+};
+__device__ __forceinline__ bool local_setup(const DevScene &sc, const DevLight &l, uint64_t mesh_id, uint32_t x,
+                                            uint32_t y, f3 pos, uint32_t first, LocalGather &g) {
     f3 to_texel = sub(pos, l.position);
     if (length_sq(to_texel) > l.radius * l.radius) return false;
-    f3 direction = normalize_or(to_texel, f3{0.0f, 1.0f, 0.0f});
-    Pcg rng = stream5(sc.seed, mesh_id, l.id, x, y);
-    uint32_t samples = l.bounce_samples;
-    float step = 0.9f / (float)(samples - 1);
-    FSum3<TR::kRefine> sum;
-    for (uint32_t i = 0; i < samples; ++i) {
-        float spread_s = 0.1f + (float)i * step;
-        f3 random = on_unit_sphere(rng);
-        f3 sample = normalize_or(slerp3(direction, random, spread_s), direction);
-        Photon ph = cube[cube_texel_index(sample, res)];
-        f3 pn{(float)(int8_t)(ph.normal & 0xFF) / 127.0f, (float)(int8_t)((ph.normal >> 8) & 0xFF) / 127.0f,
-              (float)(int8_t)((ph.normal >> 16) & 0xFF) / 127.0f};
-        pn = normalize_or_zero(pn);
-        f3 photon = add(l.position, scale(sample, ph.distance));
-        f3 albedo{(float)(ph.albedo & 0xFF) / 255.0f, (float)((ph.albedo >> 8) & 0xFF) / 255.0f,
-                  (float)((ph.albedo >> 16) & 0xFF) / 255.0f};
-        f3 to_photon = sub(photon, tr.origin);
-        float distance = length(to_photon);
-        if (is_zero(pn) || distance <= 0.0f) continue;
-        f3 d = divs(to_photon, distance);
-        ++rays;
-        if (!tr(d, distance)) {
-            float weight = fmaxf(dot(normal, d), 0.0f) * fmaxf(dot(pn, neg(d)), 0.0f);
-            sum.add(scale(reflected(sc, albedo), weight));
-        }
-    }
-    value = divs(scale(sum.value(), l.bounce_intensity), (float)samples);
+    g.direction = normalize_or(to_texel, f3{0.0f, 1.0f, 0.0f});
+    g.rng = stream5(sc.seed, mesh_id, l.id, x, y);
+    g.rng.advance(2ull * first);  // on_unit_sphere takes two draws per sample
+    g.step = 0.9f / (float)(l.bounce_samples - 1);
     return true;
 }
-
-// gather_sun's per-texel body (sun_bounce.rs:333-370).
-template <bool REFINE = false>
-__device__ __forceinline__ void gather_sun(const DevScene &sc, const DevLight &l, uint64_t mesh_id, uint32_t x,
-                                           uint32_t y, f3 origin, f3 normal, int *stack, int stride, f3 &value,
-                                           uint32_t &rays, Visits *vis = nullptr) {
-    bool alpha = (l.flags & kLightAlpha) != 0;
-    Pcg rng = stream5(sc.seed, mesh_id, l.id, x, y);
-    f2 off;
-    off.x = rng.next_f32();
-    off.y = rng.next_f32();
-    uint32_t samples = l.bounce_samples;
-    FSum3<REFINE> sum;
-    f3 side, across;
-    ortho_pair(normal, side, across);
-    for (uint32_t i = 0; i < samples; ++i) {
-        f3 direction = cosine_direction_basis(normal, side, across, spread(i, off, true));
-        ++rays;
-        Hit h;
-        if (!traverse<false, false, REFINE>(sc, origin, direction, INFINITY, alpha, stack, stride, h, vis)) continue;
-        f3 face = hit_face_normal(sc, h);
-        if (dot(face, direction) >= 0.0f) continue;
-        float lit = dot(hit_surface_normal(sc, h, face), l.toward);
-        if (lit <= 0.0f || dot(face, l.toward) <= 0.0f) continue;
-        f3 point = add(add(origin, scale(direction, h.t)), scale(face, kRayOffset));
-        ++rays;
-        if (!occluded<false, REFINE>(sc, point, l.toward, INFINITY, alpha, stack, stride, vis))
-            sum.add(scale(reflected(sc, hit_albedo(sc, h)), lit));
+// Sample i of gather_triangle (bounce.rs:267-289); `g.rng` must stand at sample i.
+template <class TR>
+__device__ __forceinline__ Contribution local_sample(const DevScene &sc, const DevLight &l, const Photon *cube,
+                                                    uint32_t res, f3 normal, LocalGather &g, uint32_t i,
+                                                    const TR &tr) {
+    Contribution c{f3{0.0f, 0.0f, 0.0f}, false, 0};
+    float spread_s = 0.1f + (float)i * g.step;
+    f3 random = on_unit_sphere(g.rng);
+    f3 sample = normalize_or(slerp3(g.direction, random, spread_s), g.direction);
+    Photon ph = cube[cube_texel_index(sample, res)];
+    f3 pn{(float)(int8_t)(ph.normal & 0xFF) / 127.0f, (float)(int8_t)((ph.normal >> 8) & 0xFF) / 127.0f,
+          (float)(int8_t)((ph.normal >> 16) & 0xFF) / 127.0f};
+    pn = normalize_or_zero(pn);
+    f3 photon = add(l.position, scale(sample, ph.distance));
+    f3 albedo{(float)(ph.albedo & 0xFF) / 255.0f, (float)((ph.albedo >> 8) & 0xFF) / 255.0f,
+              (float)((ph.albedo >> 16) & 0xFF) / 255.0f};
+    f3 to_photon = sub(photon, tr.origin);
+    float distance = length(to_photon);
+    if (is_zero(pn) || distance <= 0.0f) return c;
+    f3 d = divs(to_photon, distance);
+    c.rays = 1;
+    if (!tr(d, distance)) {
+        float weight = fmaxf(dot(normal, d), 0.0f) * fmaxf(dot(pn, neg(d)), 0.0f);
+        c.value = scale(reflected(sc, albedo), weight);
+        c.add = true;
     }
-    value = divs(scale(sum.value(), l.bounce_intensity), (float)samples);
+    return c;
+}
+
+// gather_sun's per-texel setup (sun_bounce.rs:43-52).
+struct SunGather {
+    f2 off;
+    f3 side, across;
+};
+__device__ __forceinline__ void sun_setup(const DevScene &sc, const DevLight &l, uint64_t mesh_id, uint32_t x,
+                                          uint32_t y, f3 normal, SunGather &g) {
+    Pcg rng = stream5(sc.seed, mesh_id, l.id, x, y);
+    g.off.x = rng.next_f32();
+    g.off.y = rng.next_f32();
+    ortho_pair(normal, g.side, g.across);
+}
+// Sample i of gather_sun (sun_bounce.rs:53-71).
+template <bool REFINE>
+__device__ __forceinline__ Contribution sun_sample(const DevScene &sc, const DevLight &l, f3 origin, f3 normal,
+                                                  const SunGather &g, uint32_t i, int *stack, int stride,
+                                                  Visits *vis) {
+    Contribution c{f3{0.0f, 0.0f, 0.0f}, false, 1};
+    bool alpha = (l.flags & kLightAlpha) != 0;
+    f3 direction = cosine_direction_basis(normal, g.side, g.across, spread(i, g.off, true));
+    Hit h;
+    if (!traverse<false, false, REFINE>(sc, origin, direction, INFINITY, alpha, stack, stride, h, vis)) return c;
+    f3 face = hit_face_normal(sc, h);
+    if (dot(face, direction) >= 0.0f) return c;
+    float lit = dot(hit_surface_normal(sc, h, face), l.toward);
+    if (lit <= 0.0f || dot(face, l.toward) <= 0.0f) return c;
+    f3 point = add(add(origin, scale(direction, h.t)), scale(face, kRayOffset));
+    c.rays = 2;
+    if (!occluded<false, REFINE>(sc, point, l.toward, INFINITY, alpha, stack, stride, vis)) {
+        c.value = scale(reflected(sc, hit_albedo(sc, h)), lit);
+        c.add = true;
+    }
+    return c;
 }
 
 // quantize (bounce_pack.rs:74-86)

@@ -372,6 +372,21 @@ struct Pcg {
         return (xs >> rot) | (xs << ((32u - rot) & 31u));
     }
     DL_HD float next_f32() { return (float)(next_u32() >> 8) * (1.0f / 16777216.0f); }
+    // Jumps the state `delta` draws ahead in O(log delta) (Brown, "Random Number Generation with
+    // Arbitrary Strides", 1994): the LCG step composed with itself by squaring.
+    DL_HD void advance(uint64_t delta) {
+        uint64_t mult = 6364136223846793005ull, plus = inc, acc_mult = 1, acc_plus = 0;
+        while (delta) {
+            if (delta & 1) {
+                acc_mult *= mult;
+                acc_plus = acc_plus * mult + plus;
+            }
+            plus = (mult + 1) * plus;
+            mult *= mult;
+            delta >>= 1;
+        }
+        state = acc_mult * state + acc_plus;
+    }
 };
 DL_HD Pcg pcg_new(uint64_t seed, uint64_t stream) {
     Pcg r{0, (stream << 1) | 1};

@@ -155,7 +155,8 @@ typedef struct dl_bake_config {
     uint32_t device;           /* CUDA device ordinal */
     uint32_t block_threads;    /* 0: tuned default */
     uint32_t chunk_texels;     /* (pair, texel) items a warp claims from the queue at once, 0: tuned */
-    uint32_t sample_lanes;     /* lanes sharing one sky texel's samples (1, 2, 4, 8, 16 or 32), 0: tuned */
+    uint32_t sample_lanes;     /* lanes sharing one texel's sky samples and bounce-gather samples
+                                  (1, 2, 4, 8, 16 or 32), 0: tuned */
     uint32_t blocks_per_sm;    /* upper bound of persistent blocks per SM, 0: as many as fit */
     uint32_t count_visits;     /* 1: run the instrumented visibility kernel that counts BVH node
                                   visits and triangle tests (for roofline accounting; slower) */
@@ -199,6 +200,8 @@ typedef struct dl_bake_report {
     uint32_t tuned_min_blocks;  /* launch bound: blocks per SM the registers were sized for */
     uint32_t tune_trials;       /* candidate shapes timed in this run (0: defaults or cached) */
     double ms_tune;             /* host time of those trials */
+    uint32_t tuned_gather_lanes; /* lanes sharing one texel's samples in the bounce gather */
+    uint32_t reserved_report;
 } dl_bake_report;
 
 /* LightBvhNode (src/bake/light_bvh.rs:16-22), 32 bytes. */

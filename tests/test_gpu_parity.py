@@ -208,6 +208,23 @@ def test_sky_sample_lanes_do_not_change_the_bytes(lanes):
         assert report.tuned_sample_lanes == lanes and report.tuned_chunk_texels == chunk
 
 
+@pytest.mark.parametrize("lanes", [1, 4, 16, 32])
+def test_gather_sample_lanes_do_not_change_the_bytes(lanes):
+    # lanes sharing one texel's bounce samples add them in sample order: the reference's sums
+    inp, opts = scenes.room_grid(rooms=1, lights=4, boxes_per_room=3, samples=24)
+    opts.photon_cube_resolution = 48
+    sun_inp, sun_opts = scenes.outdoor(grid=33, chunks=2, boxes=12, point_lights=2, sky_samples=16,
+                                       bounce_samples=24)
+    for case, (i, o) in enumerate(((inp, opts), (sun_inp, sun_opts))):
+        want, _, _ = oracle.bake(i, o)
+        report = dl._abi.DlBakeReport()
+        got = dl.bake(i, o, sample_lanes=lanes, report=report)
+        assert_same(got, want)
+        assert report.tuned_gather_lanes == lanes
+    refined_want = oracle.bake_ex(sun_inp, sun_opts, mode=oracle.REFINED, eps=1e-5)["scene"]
+    assert_same(dl.bake(sun_inp, sun_opts, form="refined", sample_lanes=lanes), refined_want)
+
+
 def test_autotuned_launch_shape_gives_the_default_bytes():
     # a scene with over a million queue items, so the first run times candidate shapes
     inp, opts = scenes.outdoor(grid=193, chunks=2, boxes=150, point_lights=6, sky_samples=64, bounce_samples=16)
