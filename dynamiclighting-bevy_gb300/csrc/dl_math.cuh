@@ -331,7 +331,9 @@ DL_HD double asin_series(double y) {
     p = p * y2 + 1.0;
     return y * p;
 }
-DL_HD float acos_f(float xf) {
+// acos in binary64: asin's series on |x| <= 1/2, else acos(x) = 2 asin(sqrt((1 - x) / 2)) and
+// pi - 2 asin(sqrt((1 + x) / 2)); rounded once.
+DL_HD float acos_d(float xf) {
     double x = (double)xf;
     if (isnan(x) || x > 1.0 || x < -1.0) return NAN;
     double r;
@@ -342,6 +344,57 @@ DL_HD float acos_f(float xf) {
     else
         r = kPi - 2.0 * asin_series(sqrt((1.0 + x) * 0.5));
     return (float)r;
+}
+// The same series in double-float binary32 for |y| <= 1/2: the coefficients of y^3 .. y^13 as
+// binary32 pairs, the tail (y^15 .. y^45, below 2^-17 of the result) in binary32.
+DL_HD FF ff_asin_poly(FF y) {
+    FF z2 = ff_mul(y, y);
+    float z = z2.h;
+    float t = 0.002657870529219508f;
+    t = t * z + 0.0028461783658713102f;
+    t = t * z + 0.0030578216537833214f;
+    t = t * z + 0.003297059563919902f;
+    t = t * z + 0.003569205291569233f;
+    t = t * z + 0.0038809645920991898f;
+    t = t * z + 0.00424090726301074f;
+    t = t * z + 0.00466014351695776f;
+    t = t * z + 0.005153309553861618f;
+    t = t * z + 0.005740037653595209f;
+    t = t * z + 0.006447210442274809f;
+    t = t * z + 0.007312525995075703f;
+    t = t * z + 0.008390335366129875f;
+    t = t * z + 0.009761609137058258f;
+    t = t * z + 0.01155180111527443f;
+    t = t * z + 0.013964843936264515f;
+    FF p = ff_add_f(FF{0.017352763563394547f, 8.596823808382226e-10f}, z * t);
+    p = ff_add(FF{0.022372158244252205f, 8.466569112464128e-10f}, ff_mul(z2, p));
+    p = ff_add(FF{0.0303819440305233f, 4.1392114735749885e-10f}, ff_mul(z2, p));
+    p = ff_add(FF{0.0446428582072258f, -1.0643687042843908e-09f}, ff_mul(z2, p));
+    p = ff_add(FF{0.07500000298023224f, -2.9802322831784522e-09f}, ff_mul(z2, p));
+    p = ff_add(FF{0.1666666716337204f, -4.967053879312289e-09f}, ff_mul(z2, p));
+    return ff_add(y, ff_mul(ff_mul(y, z2), p));
+}
+// acos of a binary32: the double-float path above, kept when Ziv's rounding test proves it
+// correctly rounded, else acos_d (so the value always equals acos_d's).
+DL_HD float acos_f(float x) {
+    if (!(x >= -1.0f && x <= 1.0f)) return NAN;
+    const FF pio2{1.5707963705062866f, -4.371138828673793e-08f}, pi{3.1415927410125732f, -8.742277657347586e-08f};
+    float a = fabsf(x);
+    FF r;
+    if (a <= 0.5f) {
+        r = ff_add(pio2, ff_neg(ff_asin_poly(FF{x, 0.0f})));
+    } else {
+        float t = (1.0f - a) * 0.5f;  // exact: 1 - a by Sterbenz's lemma, then a power of two
+        if (t == 0.0f) return x > 0.0f ? 0.0f : (float)kPi;  // acos_d(1) and acos_d(-1)
+        float sq = sqrtf(t);
+        FF y = ff_fast_sum(sq, fmaf(-sq, sq, t) / (sq + sq));  // sqrt(t) to ~2^-47
+        FF as = ff_asin_poly(y);
+        FF twice{as.h + as.h, as.l + as.l};
+        r = x > 0.0f ? twice : ff_add(pi, ff_neg(twice));
+    }
+    float out;
+    if (ff_rounds_to(r, out)) return out;
+    return acos_d(x);
 }
 
 constexpr float kTau = 6.28318530717958647692f;

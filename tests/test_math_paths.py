@@ -1,5 +1,5 @@
-"""The library's binary32 double-float sin/cos path must return exactly what the binary64 path
-(the oracle's) returns; its rounding test sends the undecidable cases to binary64. CPU only: the
+"""The library's binary32 double-float sin/cos and acos paths must return exactly what the
+binary64 paths (the oracle's) return; its rounding test sends the undecidable cases to binary64. CPU only: the
 same header compiles for host and device with identical IEEE operations."""
 import os
 import subprocess
@@ -14,6 +14,8 @@ def test_double_float_sincos_equals_the_binary64_path(tmp_path):
                     os.path.join(ROOT, "tests", "native", "sincos_check.cpp"), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe), "2000000"], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout
-    fields = out.stdout.split()
-    fallbacks = int(fields[-1])
-    assert fallbacks < 2000000 // 1000, out.stdout  # the binary64 path is rare
+    lines = [l.split() for l in out.stdout.splitlines() if "binary64_fallbacks" in l]
+    assert len(lines) == 2, out.stdout  # sin/cos, then acos
+    for fields in lines:
+        assert int(fields[-3]) == 0, out.stdout  # mismatches
+        assert int(fields[-1]) < 2000000 // 1000, out.stdout  # the binary64 path is rare
