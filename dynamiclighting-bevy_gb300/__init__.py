@@ -269,6 +269,23 @@ class BakedLight:
 
 
 @dataclass
+class SunMap:
+    """SunMap (src/bake/format/types.rs:115-128)."""
+    rows: np.ndarray       # (3, 4) float32: world to map space
+    resolution: int
+    texels: np.ndarray     # uint32, two unorm16 depths per word
+
+
+@dataclass
+class SkyProbes:
+    """SkyProbes (src/bake/format/types.rs:72-113)."""
+    origin: tuple
+    spacing: float
+    counts: tuple
+    words: np.ndarray      # uint32, two per probe
+
+
+@dataclass
 class BakedScene:
     settings: dict
     lights: List[BakedLight]
@@ -276,12 +293,33 @@ class BakedScene:
     meshes: List[BakedMesh]
     distance_cubes: np.ndarray
     stats: dict
+    sun_maps: List[SunMap] = field(default_factory=list)
+    sky_probes: Optional[SkyProbes] = None
 
     def words_equal(self, other: "BakedScene") -> bool:
         return (len(self.meshes) == len(other.meshes)
                 and all(a.id == b.id and a.resolution == b.resolution
                         and np.array_equal(a.triangles, b.triangles)
                         for a, b in zip(self.meshes, other.meshes)))
+
+    def maps_equal(self, other: "BakedScene") -> bool:
+        """Distance cubes, sun maps and sky probes equal bit for bit."""
+        if not np.array_equal(self.distance_cubes, other.distance_cubes):
+            return False
+        if len(self.sun_maps) != len(other.sun_maps):
+            return False
+        for a, b in zip(self.sun_maps, other.sun_maps):
+            if (a.resolution != b.resolution or not np.array_equal(a.rows.view(np.uint32), b.rows.view(np.uint32))
+                    or not np.array_equal(a.texels, b.texels)):
+                return False
+        a, b = self.sky_probes, other.sky_probes
+        if (a is None) != (b is None):
+            return False
+        if a is None:
+            return True
+        return (np.float32(a.spacing).view(np.uint32) == np.float32(b.spacing).view(np.uint32)
+                and np.array_equal(np.float32(a.origin).view(np.uint32), np.float32(b.origin).view(np.uint32))
+                and a.counts == b.counts and np.array_equal(a.words, b.words))
 
 
 def scene_from_c(s: DlBakedScene) -> BakedScene:
@@ -316,7 +354,20 @@ def scene_from_c(s: DlBakedScene) -> BakedScene:
     stats = dict(meshes=t.meshes, triangles=t.triangles, texels=t.texels, rays=t.rays,
                  lights_removed=t.lights_removed, bounce_rays=t.bounce_rays,
                  triangle_words=t.triangle_words)
-    return BakedScene(settings, lights, bvh, meshes, cubes, stats)
+
+    def words_of(ptr, n):
+        return np.ctypeslib.as_array(ptr, shape=(n,)).copy() if n else np.zeros(0, np.uint32)
+
+    sun_maps = []
+    for i in range(s.sun_map_count):
+        m = s.sun_maps[i]
+        sun_maps.append(SunMap(np.array(list(m.rows), np.float32).reshape(3, 4), m.resolution,
+                               words_of(m.texels, m.word_count)))
+    probes = None
+    if s.sky_probes:
+        p = s.sky_probes.contents
+        probes = SkyProbes(tuple(p.origin), p.spacing, tuple(p.counts), words_of(p.words, p.word_count))
+    return BakedScene(settings, lights, bvh, meshes, cubes, stats, sun_maps, probes)
 
 
 # ---- the library ------------------------------------------------------------------------------

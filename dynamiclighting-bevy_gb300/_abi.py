@@ -104,16 +104,29 @@ class DlBakedSettings(C.Structure):
                 ("max_lightmap_size", C.c_uint32), ("distance_cube_resolution", C.c_uint32)]
 
 
+class DlSunMap(C.Structure):
+    _fields_ = [("rows", C.c_float * 12), ("resolution", C.c_uint32), ("reserved", C.c_uint32),
+                ("word_count", C.c_uint64), ("texels", u32p)]
+
+
+class DlSkyProbes(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("spacing", C.c_float), ("counts", C.c_uint32 * 3),
+                ("reserved", C.c_uint32), ("word_count", C.c_uint64), ("words", u32p)]
+
+
 class DlBakedScene(C.Structure):
     _fields_ = [("settings", DlBakedSettings), ("light_count", C.c_uint64),
                 ("lights", C.POINTER(DlBakedLight)), ("light_bvh_count", C.c_uint64),
                 ("light_bvh", C.POINTER(DlLightBvhNode)), ("mesh_count", C.c_uint64),
                 ("meshes", C.POINTER(DlBakedMesh)), ("distance_cube_words", C.c_uint64),
-                ("distance_cubes", u32p), ("stats", DlBakeStats)]
+                ("distance_cubes", u32p), ("sun_map_count", C.c_uint64),
+                ("sun_maps", C.POINTER(DlSunMap)), ("sky_probes", C.POINTER(DlSkyProbes)),
+                ("stats", DlBakeStats)]
 
 
 STRUCTS = {
     "dl_alpha_texture": DlAlphaTexture, "dl_mesh": DlMesh, "dl_light": DlLight,
+    "dl_sun_map": DlSunMap, "dl_sky_probes": DlSkyProbes,
     "dl_bake_input": DlBakeInput, "dl_bake_options": DlBakeOptions, "dl_progress": DlProgress,
     "dl_bake_config": DlBakeConfig, "dl_bake_report": DlBakeReport,
     "dl_light_bvh_node": DlLightBvhNode, "dl_baked_light": DlBakedLight,

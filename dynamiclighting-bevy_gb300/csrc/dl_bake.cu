@@ -648,6 +648,124 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevScene sc, BounceArgs a) {
     if (REFINE) add_retests(a.ctr, vis.retests);
 }
 
+// ================================ maps for moving meshes =================================
+// Baked when dynamic_geometry is not LightingOnly (src/bake/baker.rs:114-152).
+
+constexpr uint32_t kCubeRes = 64;                     // DISTANCE_CUBE_RESOLUTION (distance_cubes.rs:22)
+constexpr uint64_t kProbeStream = 0x736b7970726f6265ull;  // PROBE_STREAM (sky_probes.rs:22)
+
+// bake_distance_cubes (distance_cubes.rs:29-75): one thread per word, texels 2w (low half) and
+// 2w + 1 of face f of light l; a ray from the light's centre through the texel centre, its
+// closest hit within the radius, else the radius, as f16.
+template <bool REFINE>
+__global__ void __launch_bounds__(kBlock) k_distance_cubes(DevScene sc, uint32_t lights, uint32_t *out,
+                                                           Counters *ctr) {
+    __shared__ int stack[kStack * kBlock];
+    const uint32_t per_face = kCubeRes * kCubeRes / 2;
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    Visits vis{0, 0, 0};
+    if (i < (uint64_t)lights * 6 * per_face) {
+        uint32_t l = (uint32_t)(i / (6 * per_face)), face = (uint32_t)(i / per_face % 6), w = (uint32_t)(i % per_face);
+        const DevLight &L = sc.lights[l];
+        float d[2];
+        for (uint32_t k = 0; k < 2; ++k) {
+            uint32_t texel = 2 * w + k;
+            f3 dir = cube_texel_direction(face, texel % kCubeRes, texel / kCubeRes, kCubeRes);
+            Hit h;
+            d[k] = traverse<false, false, REFINE>(sc, L.position, dir, L.radius, (L.flags & kLightAlpha) != 0,
+                                                  stack + threadIdx.x, kBlock, h, &vis)
+                       ? h.t
+                       : L.radius;
+        }
+        out[i] = f16_bits(d[1]) << 16 | f16_bits(d[0]);
+    }
+    if (REFINE) add_retests(ctr, vis.retests);
+}
+
+// bake_sun_map (sun_map.rs:25-74): one thread per word (texels 2w and 2w + 1, rows of
+// increasing y), a closest-hit ray along the sun's rays from the near plane, depth over the
+// map's depth as unorm16; a miss (or the odd texel past the end) stores 1.
+struct SunMapArgs {
+    f3 side, up, along, bmin;
+    float texel, depth;
+    uint32_t res, words, alpha;
+    uint32_t *out;
+};
+__device__ __forceinline__ uint32_t unorm16(float d) { return f2u(roundf(clampf(d, 0.0f, 1.0f) * 65535.0f)); }
+template <bool REFINE>
+__global__ void __launch_bounds__(kBlock) k_sun_map(DevScene sc, SunMapArgs a, Counters *ctr) {
+    __shared__ int stack[kStack * kBlock];
+    uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    Visits vis{0, 0, 0};
+    if (w < a.words) {
+        float d[2];
+        for (uint32_t k = 0; k < 2; ++k) {
+            uint32_t i = 2 * w + k;
+            d[k] = 1.0f;
+            if (i < a.res * a.res) {
+                float across = a.bmin.x + ((float)(i % a.res) + 0.5f) * a.texel;
+                float down = a.bmin.y + ((float)(i / a.res) + 0.5f) * a.texel;
+                f3 origin = add(add(scale(a.side, across), scale(a.up, down)), scale(a.along, a.bmin.z));
+                Hit h;
+                if (traverse<false, false, REFINE>(sc, origin, a.along, a.depth, a.alpha != 0, stack + threadIdx.x,
+                                                   kBlock, h, &vis))
+                    d[k] = h.t / a.depth;
+            }
+        }
+        a.out[w] = unorm16(d[1]) << 16 | unorm16(d[0]);
+    }
+    if (REFINE) add_retests(ctr, vis.retests);
+}
+
+// trace_probe (sky_probes.rs:83-109), one thread per (probe, axis): the sky samples around the
+// axis, each a closest hit (a hit at distance 0 counts as none); the open share and the rays
+// that reached a triangle's back.
+struct ProbeArgs {
+    f3 origin;
+    float spacing;
+    uint32_t cx, cy, alpha;
+    unsigned long long jobs;  // probes * 6
+    float *open;
+    uint32_t *back;
+};
+template <bool REFINE>
+__global__ void __launch_bounds__(kBlock) k_sky_probes(DevScene sc, ProbeArgs a, Counters *ctr) {
+    __shared__ int stack[kStack * kBlock];
+    unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    Visits vis{0, 0, 0};
+    if (i < a.jobs) {
+        uint64_t probe = i / 6;
+        uint32_t axis = (uint32_t)(i % 6);
+        uint32_t x = (uint32_t)(probe % a.cx), y = (uint32_t)(probe % ((uint64_t)a.cx * a.cy) / a.cx),
+                 z = (uint32_t)(probe / ((uint64_t)a.cx * a.cy));
+        f3 position = add(a.origin, f3{(float)x * a.spacing, (float)y * a.spacing, (float)z * a.spacing});
+        f3 normal{0.0f, 0.0f, 0.0f};
+        float sign = (axis & 1) ? -1.0f : 1.0f;
+        if (axis < 2) normal.x = sign;
+        else if (axis < 4) normal.y = sign;
+        else normal.z = sign;
+        Pcg rng = stream6(sc.seed, kProbeStream, x, y, z, axis);
+        f2 off;
+        off.x = rng.next_f32();
+        off.y = rng.next_f32();
+        f3 side, across;
+        ortho_pair(normal, side, across);
+        uint32_t open = 0, back = 0, samples = sc.sky_samples;
+        for (uint32_t taken = 0; taken < samples; ++taken) {
+            f3 dir = cosine_direction_basis(normal, side, across, spread(taken, off, true));
+            Hit h;
+            bool found = traverse<false, false, REFINE>(sc, position, dir, INFINITY, a.alpha != 0, stack + threadIdx.x,
+                                                        kBlock, h, &vis) &&
+                         h.t > 0.0f;
+            if (found && dot(hit_face_normal(sc, h), dir) > 0.0f) ++back;
+            if (!found) ++open;
+        }
+        a.open[i] = (float)open / (float)(samples > 1 ? samples : 1);
+        a.back[i] = back;
+    }
+    if (REFINE) add_retests(ctr, vis.retests);
+}
+
 // The bounce window of a (mesh, light) entry: its crops' union grown by 4 (bounce_map.rs:30-43).
 __host__ __device__ __forceinline__ Rect bounce_window(const uint32_t *r, uint32_t res) {
     uint32_t last = res - 1;
@@ -1253,8 +1371,16 @@ struct dl_session {
     const uint32_t *bounce_woff = nullptr;
     const float4 *bounce_map = nullptr;
     const uint32_t *region_rect = nullptr;
+    // last run's maps for moving meshes (device buffers in the pool)
+    const uint32_t *cube_words = nullptr;
+    uint64_t cube_word_count = 0;
+    std::vector<SunMapSetup> sun_setups;
+    std::vector<const uint32_t *> sun_texels;
+    ProbeGridSetup probe_grid;
+    const float *probe_open = nullptr;
+    const uint32_t *probe_back = nullptr;
     // batched-form graph over the visibility stage, rebuilt when the queue changes
-    cudaEvent_t marks[8] = {};  // stage boundaries of the last run
+    cudaEvent_t marks[9] = {};  // stage boundaries of the last run
     cudaGraphExec_t graph = nullptr;
     uint64_t graph_generation = ~0ull;
     unsigned long long graph_items = 0;
@@ -1656,6 +1782,80 @@ GatherTune gather_tune(dl_session &s, BounceArgs ba, uint32_t bpairs, bool refin
     return best;
 }
 
+// Distance cubes, sun maps and sky probes of the run (src/bake/baker.rs:114-152), queued on the
+// session's stream; nothing for LightingOnly.
+void bake_maps(dl_session &s, bool refine) {
+    const HostScene &h = s.host;
+    cudaStream_t st = s.stream;
+    Pool &P = s.pool;
+    s.cube_words = nullptr;
+    s.cube_word_count = 0;
+    s.sun_setups.clear();
+    s.sun_texels.clear();
+    s.probe_grid = ProbeGridSetup{};
+    s.probe_open = nullptr;
+    s.probe_back = nullptr;
+    if (s.options.dynamic_geometry == DL_GEOMETRY_LIGHTING_ONLY) return;
+    if (h.local_lights) {
+        s.cube_word_count = (uint64_t)h.local_lights * 6 * kCubeRes * kCubeRes / 2;
+        uint32_t *cubes = P.get<uint32_t>("cube_words", s.cube_word_count);
+        (refine ? k_distance_cubes<true> : k_distance_cubes<false>)<<<grid_for(s.cube_word_count), kBlock, 0, st>>>(
+            s.sc, h.local_lights, cubes, s.ctr);
+        LAUNCHED("k_distance_cubes");
+        ++s.launches;
+        s.cube_words = cubes;
+    }
+    bool any_sky = false, sky_alpha = false;
+    for (uint32_t slot = h.local_lights; slot < h.lights.size(); ++slot) {
+        const DevLight &l = h.lights[slot];
+        if (l.shape == DL_SHAPE_SKY) {
+            any_sky = true;
+            sky_alpha |= (l.flags & kLightAlpha) != 0;
+        }
+        if (l.shape != DL_SHAPE_SUN) continue;
+        SunMapSetup m = sun_map_setup(h, slot, s.options.sun_map_resolution);
+        const uint32_t *texels = nullptr;
+        if (!m.empty) {
+            SunMapArgs a{};
+            a.side = m.side;
+            a.up = m.up;
+            a.along = m.along;
+            a.bmin = m.bmin;
+            a.texel = m.texel;
+            a.depth = m.depth;
+            a.res = m.resolution;
+            a.words = (uint32_t)(((uint64_t)m.resolution * m.resolution + 1) / 2);
+            a.alpha = (l.flags & kLightAlpha) != 0;
+            a.out = P.get<uint32_t>("sun_map_" + std::to_string(s.sun_setups.size()), a.words);
+            (refine ? k_sun_map<true> : k_sun_map<false>)<<<grid_for(a.words), kBlock, 0, st>>>(s.sc, a, s.ctr);
+            LAUNCHED("k_sun_map");
+            ++s.launches;
+            texels = a.out;
+        }
+        s.sun_setups.push_back(m);
+        s.sun_texels.push_back(texels);
+    }
+    if (any_sky) {
+        s.probe_grid = sky_probe_grid(h, s.options.sky_probe_spacing);
+        if (s.probe_grid.present) {
+            ProbeArgs a{};
+            a.origin = s.probe_grid.origin;
+            a.spacing = s.probe_grid.spacing;
+            a.cx = s.probe_grid.counts[0];
+            a.cy = s.probe_grid.counts[1];
+            a.alpha = sky_alpha;
+            a.jobs = s.probe_grid.count() * 6;
+            a.open = P.get<float>("probe_open", a.jobs);
+            a.back = P.get<uint32_t>("probe_back", a.jobs);
+            (refine ? k_sky_probes<true> : k_sky_probes<false>)<<<grid_for(a.jobs), kBlock, 0, st>>>(s.sc, a, s.ctr);
+            LAUNCHED("k_sky_probes");
+            ++s.launches;
+            s.probe_open = a.open;
+            s.probe_back = a.back;
+        }
+    }
+}
+
 dl_status run(dl_session &s, dl_progress *progress) {
     DevScene &sc = s.sc;
     const uint32_t T = sc.triangles, M = sc.mesh_count, L = sc.light_count;
@@ -1697,6 +1897,8 @@ dl_status run(dl_session &s, dl_progress *progress) {
         // no triangles: every mesh serializes to no words (triangle_words.rs:47-56)
         CK(cudaEventRecord(v0, st));
         CK(cudaEventRecord(v1, st));
+        s.launches = 0;
+        bake_maps(s, refine);
         CK(cudaEventRecord(e1, st));
         CK(cudaStreamSynchronize(st));
         s.mesh_words.assign(M + 1, 0);
@@ -1706,7 +1908,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
         s.texels = 0;
         s.report.ms_device = s.report.ms_visibility = 0.0;
         s.report.pairs = 0;
-        s.report.kernel_launches = 0;
+        s.report.kernel_launches = s.launches;
         s.have_result = true;
         return DL_OK;
     }
@@ -2092,8 +2294,11 @@ dl_status run(dl_session &s, dl_progress *progress) {
             ++s.launches;
         }
     }
-    CK(cudaEventRecord(e1, st));
     CK(cudaEventRecord(s.marks[7], st));
+    // ---- maps for moving meshes
+    bake_maps(s, refine);
+    CK(cudaEventRecord(s.marks[8], st));
+    CK(cudaEventRecord(e1, st));
     s.mesh_words.resize(M + 1);
     CK(cudaMemcpyAsync(s.mesh_words.data(), mesh_words, (M + 1) * 8ull, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&s.counters, s.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
@@ -2103,7 +2308,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
     CK(cudaEventElapsedTime(&vms, v0, v1));
     s.report.ms_device = ms;
     s.report.ms_visibility = vms;
-    for (int k = 0; k < 7; ++k) {
+    for (int k = 0; k < 8; ++k) {
         float ms_k = 0.0f;
         CK(cudaEventElapsedTime(&ms_k, s.marks[k], s.marks[k + 1]));
         s.report.ms_stages[k] = ms_k;
@@ -2137,6 +2342,11 @@ struct HostResult {
     std::vector<dl_light_bvh_node> bvh;
     std::vector<dl_baked_mesh> meshes;
     std::vector<uint32_t> words;
+    std::vector<uint32_t> cubes;
+    std::vector<std::vector<uint32_t>> sun_words;
+    std::vector<dl_sun_map> sun_maps;
+    std::vector<uint32_t> probe_words;
+    dl_sky_probes probes{};
 };
 
 dl_status result(dl_session &s, dl_baked_scene *&out) {
@@ -2199,6 +2409,54 @@ dl_status result(dl_session &s, dl_baked_scene *&out) {
     sc.light_bvh = r->bvh.data();
     sc.mesh_count = r->meshes.size();
     sc.meshes = r->meshes.data();
+    // maps for moving meshes
+    if (s.cube_word_count) {
+        r->cubes.resize(s.cube_word_count);
+        CK(cudaMemcpy(r->cubes.data(), s.cube_words, s.cube_word_count * 4, cudaMemcpyDeviceToHost));
+    }
+    for (size_t i = 0; i < s.sun_setups.size(); ++i) {
+        const SunMapSetup &m = s.sun_setups[i];
+        dl_sun_map d{};
+        std::vector<uint32_t> texels;
+        if (m.empty) {
+            texels.assign(1, 0xFFFFFFFFu);  // pack_sun_depth(1, 1)
+            d.resolution = 1;
+        } else {
+            texels.resize(((uint64_t)m.resolution * m.resolution + 1) / 2);
+            CK(cudaMemcpy(texels.data(), s.sun_texels[i], texels.size() * 4, cudaMemcpyDeviceToHost));
+            d.resolution = m.resolution;
+            for (int k = 0; k < 12; ++k) d.rows[k] = m.rows[k];
+        }
+        r->sun_words.push_back(std::move(texels));
+        r->sun_maps.push_back(d);
+    }
+    for (size_t i = 0; i < r->sun_maps.size(); ++i) {
+        r->sun_maps[i].word_count = r->sun_words[i].size();
+        r->sun_maps[i].texels = r->sun_words[i].data();
+    }
+    if (s.probe_grid.present) {
+        const ProbeGridSetup &g = s.probe_grid;
+        std::vector<float> open(g.count() * 6);
+        std::vector<uint32_t> back(g.count() * 6);
+        CK(cudaMemcpy(open.data(), s.probe_open, open.size() * 4, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(back.data(), s.probe_back, back.size() * 4, cudaMemcpyDeviceToHost));
+        r->probe_words = sky_probe_words(g, open.data(), back.data(), o.sky_samples);
+        dl_sky_probes &p = r->probes;
+        p.origin[0] = g.origin.x;
+        p.origin[1] = g.origin.y;
+        p.origin[2] = g.origin.z;
+        p.spacing = g.spacing;
+        for (int k = 0; k < 3; ++k) p.counts[k] = g.counts[k];
+        p.word_count = r->probe_words.size();
+        p.words = r->probe_words.data();
+    }
+    for (const auto &w : r->sun_words) s.report.d2h_bytes += w.size() * 4;
+    s.report.d2h_bytes += r->cubes.size() * 4 + (s.probe_grid.present ? s.probe_grid.count() * 6 * 8 : 0);
+    sc.distance_cube_words = r->cubes.size();
+    sc.distance_cubes = r->cubes.empty() ? nullptr : r->cubes.data();
+    sc.sun_map_count = r->sun_maps.size();
+    sc.sun_maps = r->sun_maps.empty() ? nullptr : r->sun_maps.data();
+    sc.sky_probes = s.probe_grid.present ? &r->probes : nullptr;
     sc.stats.meshes = (uint32_t)h.meshes.size();
     sc.stats.triangles = h.triangles;
     sc.stats.texels = s.texels;

@@ -32,6 +32,7 @@ bool check_options(const dl_bake_options &o, std::string &err) {
     else if (!(std::isfinite(o.sky_probe_spacing) && o.sky_probe_spacing > 0.0f)) bad = "the sky probe spacing must be positive";
     else if (o.bounce_compression != 8 && o.bounce_compression != 6 && o.bounce_compression != 5 && o.bounce_compression != 4)
         bad = "bounce compression must be 8, 6, 5 or 4 bits";
+    else if (o.dynamic_geometry > DL_GEOMETRY_ANGULAR) bad = "unknown dynamic geometry mode";
     if (bad) err = std::string("invalid bake options: ") + bad;
     return bad == nullptr;
 }
@@ -175,10 +176,6 @@ struct LightBvhBuild {
 
 dl_status prepare_scene(const dl_bake_input &in, const dl_bake_options &o, HostScene &s, std::string &err) {
     if (!check_options(o, err)) return DL_INVALID_OPTIONS;
-    if (o.dynamic_geometry != DL_GEOMETRY_LIGHTING_ONLY) {
-        err = "distance cubes, sun maps and sky probes are not baked by this library: use LightingOnly";
-        return DL_UNSUPPORTED;
-    }
     if ((in.mesh_count && !in.meshes) || (in.light_count && !in.lights)) {
         err = "null mesh or light array";
         return DL_INVALID_ARGUMENT;
@@ -566,6 +563,140 @@ struct Writer {
 };
 }  // namespace
 
+// ---- maps for moving meshes: host halves -------------------------------------------------------
+
+// Calls f(vertex) for every corner of every occluder triangle (sun_map.rs:164-170).
+template <class F>
+static void for_occluder_vertices(const HostScene &s, F f) {
+    for (size_t i = 0; i < s.occ_mesh.size(); ++i) {
+        const dl_mesh &m = *s.meshes[s.occ_mesh[i]];
+        const uint32_t *c = m.indices + (size_t)s.occ_tri[i] * 3;
+        for (int k = 0; k < 3; ++k) {
+            const float *p = m.positions + (size_t)c[k] * 3;
+            f(f3{p[0], p[1], p[2]});
+        }
+    }
+}
+static bool finite3(f3 v) { return std::isfinite(v.x) && std::isfinite(v.y) && std::isfinite(v.z); }
+
+SunMapSetup sun_map_setup(const HostScene &s, uint32_t slot, uint32_t resolution) {
+    SunMapSetup m;
+    f3 toward = s.lights[slot].toward;
+    ortho_pair(toward, m.side, m.up);
+    m.along = neg(toward);
+    f3 mn{INFINITY, INFINITY, INFINITY}, mx{-INFINITY, -INFINITY, -INFINITY};
+    for_occluder_vertices(s, [&](f3 v) {
+        f3 l{dot(v, m.side), dot(v, m.up), dot(v, m.along)};
+        mn = vmin(mn, l);
+        mx = vmax(mx, l);
+    });
+    if (!(finite3(mn) && finite3(mx))) return m;  // empty: rows zero, one texel
+    m.empty = false;
+    f3 size = sub(mx, mn);
+    float margin = size.z * 0.01f + 0.05f;  // DEPTH_MARGIN (sun_map.rs:20-22)
+    m.extent = fmaxf(size.x, size.y) + 2.0f * margin;
+    f3 center = scale(add(mn, mx), 0.5f);
+    m.bmin = f3{center.x - m.extent * 0.5f, center.y - m.extent * 0.5f, mn.z - margin};
+    m.depth = size.z + 2.0f * margin;
+    auto row = [](float *r, f3 axis, float lo, float length) {
+        f3 a = divs(axis, length);
+        r[0] = a.x;
+        r[1] = a.y;
+        r[2] = a.z;
+        r[3] = -lo / length;
+    };
+    row(m.rows, m.side, m.bmin.x, m.extent);
+    row(m.rows + 4, m.up, m.bmin.y, m.extent);
+    row(m.rows + 8, m.along, m.bmin.z, m.depth);
+    m.resolution = resolution;
+    m.texel = m.extent / (float)resolution;
+    return m;
+}
+
+ProbeGridSetup sky_probe_grid(const HostScene &s, float spacing) {
+    ProbeGridSetup g;
+    if (s.occ_mesh.empty()) return g;
+    bool first = true;
+    f3 mn{0, 0, 0}, mx{0, 0, 0};
+    for_occluder_vertices(s, [&](f3 v) {
+        if (first) {
+            mn = mx = v;
+            first = false;
+        } else {
+            mn = vmin(mn, v);
+            mx = vmax(mx, v);
+        }
+    });
+    // ProbeGrid::over (sky_probes.rs:45-61), MAX_SKY_PROBES = 65536 (:18)
+    f3 extent = add(vmax(sub(mx, mn), f3{0, 0, 0}), f3{spacing, spacing, spacing});
+    auto counts_at = [&](float sp) {
+        g.counts[0] = f2u(ceilf(extent.x / sp)) + 1;
+        g.counts[1] = f2u(ceilf(extent.y / sp)) + 1;
+        g.counts[2] = f2u(ceilf(extent.z / sp)) + 1;
+    };
+    counts_at(spacing);
+    while (g.count() > 65536) {
+        float ratio = (float)g.count() / 65536.0f;
+        spacing = spacing * fmaxf((float)std::cbrt((double)ratio), 1.01f);  // f32::cbrt, rounded once
+        counts_at(spacing);
+    }
+    f3 span{(float)(g.counts[0] - 1) * spacing, (float)(g.counts[1] - 1) * spacing,
+            (float)(g.counts[2] - 1) * spacing};
+    g.origin = sub(scale(add(mn, mx), 0.5f), scale(span, 0.5f));
+    g.spacing = spacing;
+    g.present = true;
+    return g;
+}
+
+std::vector<uint32_t> sky_probe_words(const ProbeGridSetup &g, const float *open, const uint32_t *back,
+                                      uint32_t samples) {
+    const uint64_t n = g.count();
+    const int cx = (int)g.counts[0], cy = (int)g.counts[1], cz = (int)g.counts[2];
+    std::vector<float> values(n * 6);
+    std::vector<uint8_t> valid(n);
+    const float rays = (float)(std::max(samples, 1u) * 6u);
+    for (uint64_t i = 0; i < n; ++i) {
+        uint32_t b = 0;
+        for (int a = 0; a < 6; ++a) b += back[i * 6 + a];
+        valid[i] = (float)b <= 0.25f * rays;  // INSIDE_SHARE (sky_probes.rs:20)
+        for (int a = 0; a < 6; ++a) values[i * 6 + a] = open[i * 6 + a];
+    }
+    static const int STEP[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+    for (;;) {  // fill_inside: layer by layer from the previous pass
+        std::vector<float> pv = values;
+        std::vector<uint8_t> pok = valid;
+        bool changed = false;
+        for (uint64_t i = 0; i < n; ++i) {
+            if (pok[i]) continue;
+            int x = (int)(i % (uint64_t)cx), y = (int)(i % ((uint64_t)cx * cy) / (uint64_t)cx),
+                z = (int)(i / ((uint64_t)cx * cy));
+            float sum[6] = {0, 0, 0, 0, 0, 0}, found = 0.0f;
+            for (const auto &st : STEP) {
+                int nx = x + st[0], ny = y + st[1], nz = z + st[2];
+                if (nx < 0 || ny < 0 || nz < 0 || nx >= cx || ny >= cy || nz >= cz) continue;
+                uint64_t j = ((uint64_t)nz * cy + ny) * cx + nx;
+                if (!pok[j]) continue;
+                for (int a = 0; a < 6; ++a) sum[a] = sum[a] + pv[j * 6 + a];
+                found = found + 1.0f;
+            }
+            if (found > 0.0f) {
+                for (int a = 0; a < 6; ++a) values[i * 6 + a] = sum[a] / found;
+                valid[i] = 1;
+                changed = true;
+            }
+        }
+        if (!changed) break;
+    }
+    std::vector<uint32_t> words(n * 2, 0);
+    for (uint64_t i = 0; i < n; ++i)
+        for (int a = 0; a < 6; ++a) {
+            float v = valid[i] ? values[i * 6 + a] : 1.0f;
+            uint32_t byte = f2u(roundf(clampf(v, 0.0f, 1.0f) * 255.0f));
+            words[i * 2 + a / 4] |= byte << (8 * (a % 4));
+        }
+    return words;
+}
+
 std::vector<uint8_t> encode_payload(const dl_baked_scene &s) {
     Writer w;
     w.u32((s.settings.bounce ? 1u : 0u) | (s.settings.colored_bounce ? 2u : 0u));
@@ -596,8 +727,22 @@ std::vector<uint8_t> encode_payload(const dl_baked_scene &s) {
         w.words(m.triangles, m.word_count);
     }
     w.words(s.distance_cubes, s.distance_cube_words);
-    w.u64(0);  // sun maps: none in LightingOnly
-    w.u32(0);  // no sky probes
+    // maps::encode (format/maps.rs:16-38)
+    w.u64(s.sun_map_count);
+    for (uint64_t i = 0; i < s.sun_map_count; ++i) {
+        const dl_sun_map &m = s.sun_maps[i];
+        w.u32(m.resolution);
+        for (float r : m.rows) w.f32(r);
+        w.words(m.texels, m.word_count);
+    }
+    w.u32(s.sky_probes ? 1u : 0u);
+    if (s.sky_probes) {
+        const dl_sky_probes &p = *s.sky_probes;
+        for (float v : p.origin) w.f32(v);
+        w.f32(p.spacing);
+        for (uint32_t c : p.counts) w.u32(c);
+        w.words(p.words, p.word_count);
+    }
     w.u32(s.stats.meshes);
     w.u64(s.stats.triangles);
     w.u64(s.stats.texels);

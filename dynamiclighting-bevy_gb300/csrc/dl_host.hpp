@@ -82,6 +82,31 @@ dl_status prepare_scene(const dl_bake_input &in, const dl_bake_options &o, HostS
 // Builds the occluder BVH (binned SAH, leaves of at most 4 triangles, depth capped at 60).
 void build_bvh(HostScene &s);
 
+// A sun map's frame and bounds (src/bake/sun_map.rs:25-45,83-161): `empty` when there is no
+// static geometry (one texel that nothing is behind).
+struct SunMapSetup {
+    bool empty = true;
+    f3 side, up, along, bmin;
+    float extent = 0.0f, depth = 0.0f, texel = 0.0f;
+    float rows[12] = {};
+    uint32_t resolution = 1;
+};
+SunMapSetup sun_map_setup(const HostScene &s, uint32_t slot, uint32_t resolution);
+
+// The sky probe grid over the static bounds (src/bake/sky_probes.rs:45-80, 146-162).
+struct ProbeGridSetup {
+    bool present = false;
+    f3 origin;
+    float spacing = 0.0f;
+    uint32_t counts[3] = {0, 0, 0};
+    uint64_t count() const { return (uint64_t)counts[0] * counts[1] * counts[2]; }
+};
+ProbeGridSetup sky_probe_grid(const HostScene &s, float spacing);
+// The probes' words from each (probe, axis)'s open fraction and back-face hits: the inside
+// test (sky_probes.rs:104-108), fill_inside (:114-146) and SkyProbes::pack (format/types.rs:105).
+std::vector<uint32_t> sky_probe_words(const ProbeGridSetup &g, const float *open, const uint32_t *back,
+                                      uint32_t samples);
+
 // The .dynlight payload (src/bake/format/mod.rs:170-213) and its CRC-32.
 std::vector<uint8_t> encode_payload(const dl_baked_scene &scene);
 uint32_t crc32_ieee(const uint8_t *data, size_t n);

@@ -13,6 +13,7 @@
 
 #include <cstdint>
 #include <math.h>
+#include <string.h>
 
 #if defined(__CUDACC__)
 #define DL_HD __host__ __device__ __forceinline__
@@ -87,6 +88,29 @@ struct FSum3 {
     }
     DL_HD f3 value() const { return f3{x.s, y.s, z.s}; }
 };
+
+// binary32 -> binary16 bits, round to nearest even (IEEE 754; the distance cubes' f16 packing,
+// src/bake/distance_cubes.rs:23-26)
+DL_HD uint32_t f16_bits(float f) {
+    uint32_t x;
+    memcpy(&x, &f, 4);
+    uint32_t sign = (x >> 16) & 0x8000u, a = x & 0x7FFFFFFFu;
+    if (a > 0x7F800000u) return sign | 0x7E00u | ((a >> 13) & 0x3FFu);  // NaN
+    if (a >= 0x477FF000u) return sign | 0x7C00u;                      // 65520 and up: infinity
+    int e = (int)(a >> 23) - 127;
+    if (e >= -14) {
+        uint32_t h = ((uint32_t)(e + 15) << 10) | ((a >> 13) & 0x3FFu), rest = a & 0x1FFFu;
+        if (rest > 0x1000u || (rest == 0x1000u && (h & 1u))) ++h;
+        return sign | h;
+    }
+    if (a == 0) return sign;
+    int shift = -e - 1;  // half subnormals: value / 2^-24 = mantissa * 2^(e + 1)
+    if (shift > 24) return sign;
+    uint32_t mant = (a & 0x7FFFFFu) | 0x800000u;
+    uint32_t q = mant >> shift, rest = mant & ((1u << shift) - 1u), half = 1u << (shift - 1);
+    if (rest > half || (rest == half && (q & 1u))) ++q;
+    return sign | q;
+}
 
 DL_HD float fminr(float a, float b) { return fminf(a, b); }
 DL_HD float fmaxr(float a, float b) { return fmaxf(a, b); }

@@ -256,8 +256,29 @@ typedef struct dl_baked_settings {
     uint32_t distance_cube_resolution;
 } dl_baked_settings;
 
-/* BakedScene (src/bake/format/types.rs:13-37). Sun maps and sky probes are not baked here:
- * with DL_GEOMETRY_LIGHTING_ONLY the reference leaves them empty too (src/bake/baker.rs:114-152). */
+/* SunMap (src/bake/format/types.rs:115-128): map space coordinate i of world point p is
+ * rows[4i..4i+2] . p + rows[4i+3]; `resolution`^2 unorm16 depths, two per word (texel 2k low). */
+typedef struct dl_sun_map {
+    float rows[12];
+    uint32_t resolution;
+    uint32_t reserved;
+    uint64_t word_count;
+    const uint32_t *texels;
+} dl_sun_map;
+
+/* SkyProbes (src/bake/format/types.rs:72-113): probe (x, y, z) at origin + spacing * (x, y, z),
+ * two words per probe (x fastest), the openness of +X, -X, +Y, -Y, +Z, -Z as unorm8. */
+typedef struct dl_sky_probes {
+    float origin[3];
+    float spacing;
+    uint32_t counts[3];
+    uint32_t reserved;
+    uint64_t word_count;
+    const uint32_t *words;
+} dl_sky_probes;
+
+/* BakedScene (src/bake/format/types.rs:13-37). With DL_GEOMETRY_LIGHTING_ONLY the distance
+ * cubes, sun maps and sky probes are empty, as in the reference (src/bake/baker.rs:114-152). */
 typedef struct dl_baked_scene {
     dl_baked_settings settings;
     uint64_t light_count;
@@ -266,8 +287,11 @@ typedef struct dl_baked_scene {
     const dl_light_bvh_node *light_bvh;
     uint64_t mesh_count;
     const dl_baked_mesh *meshes;
-    uint64_t distance_cube_words;
+    uint64_t distance_cube_words;   /* 6 x 64^2 f16 distances per local light, two per word */
     const uint32_t *distance_cubes;
+    uint64_t sun_map_count;         /* one per sun in light order, or none */
+    const dl_sun_map *sun_maps;
+    const dl_sky_probes *sky_probes; /* NULL: none */
     dl_bake_stats stats;
 } dl_baked_scene;
 

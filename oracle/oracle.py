@@ -54,6 +54,11 @@ def lib():
         _lib.oracle_captured_map.argtypes = [C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.c_uint32]
         _lib.oracle_captured_map_count.restype = C.c_uint32
+        _lib.oracle_f16_bits.restype = C.c_uint16
+        _lib.oracle_f16_bits.argtypes = [C.c_float]
+        _lib.oracle_probe_grid.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p,
+                                           C.c_void_p]
+        _lib.oracle_fill_inside.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.oracle_capture_all_bounce.argtypes = [C.c_uint32]
     return _lib
 

@@ -17,7 +17,7 @@
 #include <mutex>
 #include <string>
 
-#include "oracle_bounce.hpp"
+#include "oracle_maps.hpp"
 
 namespace oracle {
 
@@ -38,6 +38,7 @@ static bool validate_options(const dl_bake_options &o, Error &e) {
     if (!(std::isfinite(o.sky_probe_spacing) && o.sky_probe_spacing > 0.0f)) return bad("the sky probe spacing must be positive");
     if (!(o.bounce_compression == 8 || o.bounce_compression == 6 || o.bounce_compression == 5 || o.bounce_compression == 4))
         return bad("bounce compression must be 8, 6, 5 or 4 bits");
+    if (o.dynamic_geometry > DL_GEOMETRY_ANGULAR) return bad("unknown dynamic geometry mode");
     return true;
 }
 static bool validate_mesh(const dl_mesh &m, Error &e) {
@@ -723,16 +724,17 @@ struct Result {
     std::vector<dl_light_bvh_node> bvh;
     std::vector<dl_baked_mesh> meshes;
     std::vector<std::vector<uint32_t>> words;
+    std::vector<uint32_t> distance_cubes;
+    std::vector<SunMapOut> sun_map_data;
+    std::vector<dl_sun_map> sun_maps;
+    SkyProbesOut probes;
+    dl_sky_probes sky_probes{};
     uint64_t burial_rays = 0, photon_rays = 0;
 };
 
 static bool bake(const dl_bake_input &in, const dl_bake_options &o, const dl_progress *progress, bool brute,
                  Result &res, Error &err) {
     if (!validate_options(o, err)) return false;
-    if (o.dynamic_geometry != DL_GEOMETRY_LIGHTING_ONLY) {
-        err = Error{DL_UNSUPPORTED, "distance cubes, sun maps and sky probes are not baked: use LightingOnly"};
-        return false;
-    }
     // sorted_meshes / sorted_lights (baker.rs:205-233)
     std::vector<const dl_mesh *> meshes;
     for (uint64_t i = 0; i < in.mesh_count; ++i) meshes.push_back(&in.meshes[i]);
@@ -850,6 +852,44 @@ static bool bake(const dl_bake_input &in, const dl_bake_options &o, const dl_pro
         res.lights.push_back(b);
     }
     res.bvh = sc.light_bvh.nodes;
+    // distance cubes, sun maps, sky probes (baker.rs:114-152)
+    if (o.dynamic_geometry != DL_GEOMETRY_LIGHTING_ONLY) {
+        res.distance_cubes = bake_distance_cubes(sc.lights, sc.local_lights, sc.occluders);
+        bool any_sky = false, sky_alpha = false;
+        for (size_t s = sc.local_lights; s < sc.lights.size(); ++s) {
+            const Light &l = sc.lights[s];
+            if (l.l->shape == DL_SHAPE_SUN)
+                res.sun_map_data.push_back(bake_sun_map(sc.sun_toward[s], sc.occluders, o.sun_map_resolution,
+                                                        l.alpha_tested()));
+            if (l.l->shape == DL_SHAPE_SKY) {
+                any_sky = true;
+                sky_alpha |= l.alpha_tested();
+            }
+        }
+        if (any_sky) res.probes = bake_sky_probes(sc.occluders, o.sky_probe_spacing, o.sky_samples, sky_alpha, o.seed);
+        if (sc.cancelled()) {
+            err = Error{DL_CANCELLED, "the bake was cancelled"};
+            return false;
+        }
+    }
+    for (auto &m : res.sun_map_data) {
+        dl_sun_map d{};
+        for (int k = 0; k < 12; ++k) d.rows[k] = m.rows[k];
+        d.resolution = m.resolution;
+        d.word_count = m.texels.size();
+        d.texels = m.texels.data();
+        res.sun_maps.push_back(d);
+    }
+    if (res.probes.present) {
+        dl_sky_probes &p = res.sky_probes;
+        p.origin[0] = res.probes.origin.x;
+        p.origin[1] = res.probes.origin.y;
+        p.origin[2] = res.probes.origin.z;
+        p.spacing = res.probes.spacing;
+        for (int k = 0; k < 3; ++k) p.counts[k] = res.probes.counts[k];
+        p.word_count = res.probes.words.size();
+        p.words = res.probes.words.data();
+    }
     for (auto &out : outs) {
         res.words.push_back(std::move(out.words));
         res.meshes.push_back(out.mesh);
@@ -872,6 +912,11 @@ static bool bake(const dl_bake_input &in, const dl_bake_options &o, const dl_pro
     s.light_bvh = res.bvh.data();
     s.mesh_count = res.meshes.size();
     s.meshes = res.meshes.data();
+    s.distance_cube_words = res.distance_cubes.size();
+    s.distance_cubes = res.distance_cubes.data();
+    s.sun_map_count = res.sun_maps.size();
+    s.sun_maps = res.sun_maps.data();
+    s.sky_probes = res.probes.present ? &res.sky_probes : nullptr;
     s.stats = stats;
     return true;
 }
@@ -1124,6 +1169,33 @@ uint64_t oracle_intersect_batch(uint32_t mode, float eps, uint32_t n, const floa
     }
     precision() = PrecisionMode{};
     return retest_count().load();
+}
+// f32 -> f16 bits of the distance cubes' packing.
+uint16_t oracle_f16_bits(float f) { return f16_bits(f); }
+// ProbeGrid::over (sky_probes.rs:45-61): origin, spacing and counts of the probe grid.
+void oracle_probe_grid(const float mn[3], const float mx[3], float spacing, float origin[3], float *out_spacing,
+                       uint32_t counts[3]) {
+    ProbeGrid g = ProbeGrid::over(V3{mn[0], mn[1], mn[2]}, V3{mx[0], mx[1], mx[2]}, spacing);
+    origin[0] = g.origin.x;
+    origin[1] = g.origin.y;
+    origin[2] = g.origin.z;
+    *out_spacing = g.spacing;
+    for (int k = 0; k < 3; ++k) counts[k] = g.counts[k];
+}
+// fill_inside (sky_probes.rs:114-146) on a grid of `counts`: values 6 per probe, valid 0/1, in place.
+void oracle_fill_inside(const uint32_t counts[3], float *values, uint8_t *valid) {
+    ProbeGrid g{};
+    for (int k = 0; k < 3; ++k) g.counts[k] = counts[k];
+    uint64_t n = g.count();
+    std::vector<std::array<float, 6>> v(n);
+    std::vector<uint8_t> ok(valid, valid + n);
+    for (uint64_t i = 0; i < n; ++i)
+        for (int k = 0; k < 6; ++k) v[i][k] = values[i * 6 + k];
+    fill_inside(g, v, ok);
+    for (uint64_t i = 0; i < n; ++i) {
+        valid[i] = ok[i];
+        for (int k = 0; k < 6; ++k) values[i * 6 + k] = v[i][k];
+    }
 }
 // Area-light visibility of one texel with a callback `blocked(dir, distance)`; the shape is the
 // light's rotation and size at `center`. Returns 1 with fraction/rays, or 0 for None.
