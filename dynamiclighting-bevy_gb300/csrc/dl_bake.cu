@@ -562,9 +562,10 @@ struct BounceArgs {
 // lanes per (bounce pair, texel) item. Each round, lane k of a group evaluates sample
 // round * lanes + k; the group leader then adds the round's contributions in sample order, so
 // the sum is the reference's sequential one for any group size. Dynamic shared memory holds the
-// traversal stacks and one float4 contribution slot per thread.
-template <bool REFINE>
-__global__ void __launch_bounds__(kBlock) k_gather(DevScene sc, BounceArgs a) {
+// traversal stacks and one float4 contribution slot per thread. MINB is the launch bound's
+// blocks per SM (the register budget: 6 leaves the compiler its 80 registers, 8 asks for 64).
+template <bool REFINE, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs a) {
     extern __shared__ int smem[];
     int *my = smem + threadIdx.x;
     float4 *part = reinterpret_cast<float4 *>(smem + (size_t)a.stack_depth * kBlock);
@@ -1717,9 +1718,14 @@ TraceTune trace_tune(dl_session &s, TraceArgs ta, bool refine, bool count, dl_pr
 // The gather kernel's lanes per texel, tuned the same way (trials on every k-th step of the real
 // item list, value writes that the real pass overwrites).
 struct GatherTune {
-    uint32_t lanes = 1, stack_depth = kStack, blocks = 1, trials = 0;
+    uint32_t lanes = 1, minb = 6, stack_depth = kStack, blocks = 1, trials = 0;
     double ms = 0.0;
 };
+using GatherKernel = void (*)(DevScene, BounceArgs);
+GatherKernel gather_kernel(bool refine, uint32_t minb) {
+    if (refine) return k_gather<true, 6>;
+    return minb == 8 ? k_gather<false, 8> : k_gather<false, 6>;
+}
 size_t gather_smem(uint32_t depth) { return (size_t)depth * kBlock * sizeof(int) + kBlock * sizeof(float4); }
 std::map<TuneKey, GatherTune> g_gather_cache;
 
@@ -1727,16 +1733,22 @@ GatherTune gather_tune(dl_session &s, BounceArgs ba, uint32_t bpairs, bool refin
     const dl_bake_config &c = s.config;
     GatherTune best;
     best.stack_depth = std::max<uint32_t>(8, (s.host.bvh_depth + 3) & ~3u);
-    auto kernel = refine ? k_gather<true> : k_gather<false>;
-    int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, gather_smem(best.stack_depth)));
-    if (c.blocks_per_sm) per_sm = std::min(per_sm, (int)c.blocks_per_sm);
-    best.blocks = (uint32_t)std::max(1, per_sm) * (uint32_t)s.sms;
+    auto blocks_for = [&](uint32_t minb) {
+        int per_sm = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gather_kernel(refine, minb), kBlock,
+                                                         gather_smem(best.stack_depth)));
+        if (c.blocks_per_sm) per_sm = std::min(per_sm, (int)c.blocks_per_sm);
+        return (uint32_t)std::max(1, per_sm) * (uint32_t)s.sms;
+    };
     std::vector<uint32_t> lanes = c.sample_lanes ? std::vector<uint32_t>{c.sample_lanes}
                                                  : std::vector<uint32_t>{1, 4, 8, 16};
+    std::vector<uint32_t> minbs = refine ? std::vector<uint32_t>{6} : std::vector<uint32_t>{6, 8};
     const uint32_t every = ba.items >= (1u << 20) ? 8 : ba.items >= (1u << 18) ? 4 : 0;
     best.lanes = lanes[0];
-    if (c.no_autotune || !every || lanes.size() == 1 || (progress && progress->cancel)) return best;
+    best.minb = minbs[0];
+    best.blocks = blocks_for(best.minb);
+    if (c.no_autotune || !every || lanes.size() * minbs.size() == 1 || (progress && progress->cancel))
+        return best;
     TuneKey key{s.device, ba.items, bpairs, 0, s.host.tri_v0.size(), s.host.nodes.size(), best.stack_depth,
                 refine ? 2u : 0u, c.blocks_per_sm};
     {
@@ -1758,20 +1770,25 @@ GatherTune gather_tune(dl_session &s, BounceArgs ba, uint32_t bpairs, bool refin
     CK(cudaEventCreate(&b));
     float best_ms = INFINITY;
     auto t0 = std::chrono::steady_clock::now();
-    for (uint32_t w : lanes) {
-        ba.lanes = w;
-        CK(cudaMemsetAsync(ba.head, 0, sizeof(unsigned long long), st));
-        CK(cudaEventRecord(a, st));
-        kernel<<<best.blocks, kBlock, gather_smem(best.stack_depth), st>>>(s.sc, ba);
-        CK(cudaGetLastError());
-        CK(cudaEventRecord(b, st));
-        CK(cudaEventSynchronize(b));
-        float ms = 0.0f;
-        CK(cudaEventElapsedTime(&ms, a, b));
-        ++best.trials;
-        if (ms < best_ms) {
-            best_ms = ms;
-            best.lanes = w;
+    for (uint32_t minb : minbs) {
+        uint32_t blocks = blocks_for(minb);
+        for (uint32_t w : lanes) {
+            ba.lanes = w;
+            CK(cudaMemsetAsync(ba.head, 0, sizeof(unsigned long long), st));
+            CK(cudaEventRecord(a, st));
+            gather_kernel(refine, minb)<<<blocks, kBlock, gather_smem(best.stack_depth), st>>>(s.sc, ba);
+            CK(cudaGetLastError());
+            CK(cudaEventRecord(b, st));
+            CK(cudaEventSynchronize(b));
+            float ms = 0.0f;
+            CK(cudaEventElapsedTime(&ms, a, b));
+            ++best.trials;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best.lanes = w;
+                best.minb = minb;
+                best.blocks = blocks;
+            }
         }
     }
     cudaEventDestroy(a);
@@ -2191,7 +2208,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
             s.report.tune_trials += g.trials;
             s.report.ms_tune += g.ms;
             CK(cudaMemsetAsync(ba.head, 0, sizeof(unsigned long long), st));
-            (refine ? k_gather<true> : k_gather<false>)<<<g.blocks, kBlock, gather_smem(g.stack_depth), st>>>(sc, ba);
+            gather_kernel(refine, g.minb)<<<g.blocks, kBlock, gather_smem(g.stack_depth), st>>>(sc, ba);
             LAUNCHED("k_gather");
             ++s.launches;
         }
