@@ -238,9 +238,10 @@ def main():
     achieved = alg_bytes / (vis / 1e3) / 1e9 if vis > 0 else 0.0
     traffic = None
     traffic_path = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(traffic_path):
+    if os.path.exists(traffic_path):  # DRAM bytes per launch from an ncu capture (profiles/)
         with open(traffic_path) as f:
-            traffic = json.load(f).get(args.workload)
+            entry = json.load(f).get(args.workload)
+        traffic = entry["bytes_per_launch"] if entry else None
 
     # end to end through the C ABI (dl_bake_ex) from host buffers: validation, BVH build,
     # uploads, the device pipeline and the download of every mesh's words, timed around the call
