@@ -3,6 +3,8 @@
 #include "dl_host.hpp"
 
 #include <algorithm>
+#include <memory>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -345,6 +347,25 @@ constexpr uint32_t kMaxDepth = 60;
 // Subtrees larger than this, near the root, are built on their own threads.
 constexpr uint32_t kParallelPrims = 16384;
 constexpr uint32_t kParallelDepth = 6;
+// Nodes with more primitives than this bin and partition them with several threads.
+constexpr uint32_t kWidePrims = 65536;
+
+// Runs f(begin, end) over [first, first + count) split into one chunk per thread.
+template <class F>
+void par_chunks(uint32_t first, uint32_t count, unsigned threads, F f) {
+    if (threads <= 1) {
+        f(first, first + count, 0u);
+        return;
+    }
+    std::vector<std::thread> pool;
+    uint32_t per = (count + threads - 1) / threads;
+    for (unsigned t = 1; t < threads; ++t) {
+        uint32_t b = first + std::min(count, t * per), e = first + std::min(count, (t + 1) * per);
+        pool.emplace_back([=, &f] { f(b, e, t); });
+    }
+    f(first, first + std::min(count, per), 0u);
+    for (auto &th : pool) th.join();
+}
 
 struct Builder {
     std::vector<Prim> prims;
@@ -365,11 +386,9 @@ struct Builder {
     // Builds the subtree over idx[first, first + count) into `nodes`; `max_depth` collects the
     // deepest level. The two children of a large node near the root build concurrently, the
     // second into its own node array that is then appended with its inner references moved.
-    Ref build(std::vector<BvhNode> &nodes, uint32_t first, uint32_t count, uint32_t depth, uint32_t &max_depth) {
-        max_depth = std::max(max_depth, depth);
-        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-        float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
-        for (uint32_t k = first; k < first + count; ++k) {
+    // Bounds of the primitives' boxes and centroids over idx[b, e).
+    void bounds(uint32_t b, uint32_t e, float lo[3], float hi[3], float clo[3], float chi[3]) const {
+        for (uint32_t k = b; k < e; ++k) {
             const Prim &p = prims[idx[k]];
             for (int a = 0; a < 3; ++a) {
                 lo[a] = std::min(lo[a], p.lo[a]);
@@ -378,24 +397,100 @@ struct Builder {
                 chi[a] = std::max(chi[a], p.c[a]);
             }
         }
+    }
+    // Per-axis bins (boxes and counts) of idx[b, e) for centroid bounds clo .. clo + kBins / k.
+    struct Bins {
+        float bl[3][kBins][3], bh[3][kBins][3];
+        uint32_t bc[3][kBins];
+        void reset() {
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < kBins; ++b) {
+                    bc[a][b] = 0;
+                    for (int j = 0; j < 3; ++j) { bl[a][b][j] = INFINITY; bh[a][b][j] = -INFINITY; }
+                }
+        }
+        void merge(const Bins &o) {
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < kBins; ++b) {
+                    bc[a][b] += o.bc[a][b];
+                    for (int j = 0; j < 3; ++j) {
+                        bl[a][b][j] = std::min(bl[a][b][j], o.bl[a][b][j]);
+                        bh[a][b][j] = std::max(bh[a][b][j], o.bh[a][b][j]);
+                    }
+                }
+        }
+    };
+    void bin(uint32_t b, uint32_t e, const float clo[3], const float k[3], const bool use[3], Bins &out) const {
+        for (uint32_t i = b; i < e; ++i) {
+            const Prim &p = prims[idx[i]];
+            for (int a = 0; a < 3; ++a) {
+                if (!use[a]) continue;
+                int bb = std::min(kBins - 1, (int)((p.c[a] - clo[a]) * k[a]));
+                ++out.bc[a][bb];
+                for (int j = 0; j < 3; ++j) {
+                    out.bl[a][bb][j] = std::min(out.bl[a][bb][j], p.lo[j]);
+                    out.bh[a][bb][j] = std::max(out.bh[a][bb][j], p.hi[j]);
+                }
+            }
+        }
+    }
+
+    Ref build(std::vector<BvhNode> &nodes, uint32_t first, uint32_t count, uint32_t depth, uint32_t &max_depth) {
+        max_depth = std::max(max_depth, depth);
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        // min and max are exact, so the split bounds do not depend on how the work is divided
+        // the threads of a level share the machine: subtrees above kParallelPrims already run
+        // concurrently, 2^depth of them
+        static const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        const unsigned wide = count > kWidePrims && depth < 16 ? std::max(1u, hw >> std::min(depth - 1, 15u)) : 1u;
+        if (wide > 1) {
+            std::vector<std::array<float, 12>> part(wide);
+            par_chunks(first, count, wide, [&](uint32_t b, uint32_t e, unsigned t) {
+                float l[3] = {INFINITY, INFINITY, INFINITY}, h[3] = {-INFINITY, -INFINITY, -INFINITY};
+                float cl[3] = {INFINITY, INFINITY, INFINITY}, ch[3] = {-INFINITY, -INFINITY, -INFINITY};
+                bounds(b, e, l, h, cl, ch);
+                for (int a = 0; a < 3; ++a) {
+                    part[t][a] = l[a]; part[t][3 + a] = h[a]; part[t][6 + a] = cl[a]; part[t][9 + a] = ch[a];
+                }
+            });
+            for (const auto &q : part)
+                for (int a = 0; a < 3; ++a) {
+                    lo[a] = std::min(lo[a], q[a]); hi[a] = std::max(hi[a], q[3 + a]);
+                    clo[a] = std::min(clo[a], q[6 + a]); chi[a] = std::max(chi[a], q[9 + a]);
+                }
+        } else {
+            bounds(first, first + count, lo, hi, clo, chi);
+        }
         if (count <= 2 || (depth >= kMaxDepth && count <= 7)) return leaf(first, count, lo, hi);
         // SAH over kBins bins per axis
+        float kk[3];
+        bool use[3];
+        for (int a = 0; a < 3; ++a) {
+            float ext = chi[a] - clo[a];
+            use[a] = ext > 0.0f;
+            kk[a] = use[a] ? (float)kBins / ext : 0.0f;
+        }
+        Bins bins;
+        Bins *all = &bins;
+        all->reset();
+        if (wide > 1) {
+            std::vector<Bins> part(wide);
+            par_chunks(first, count, wide, [&](uint32_t b, uint32_t e, unsigned t) {
+                part[t].reset();
+                bin(b, e, clo, kk, use, part[t]);
+            });
+            for (auto &q : part) all->merge(q);
+        } else {
+            bin(first, first + count, clo, kk, use, *all);
+        }
         float best_cost = INFINITY;
         int best_axis = -1, best_bin = 0;
         for (int a = 0; a < 3; ++a) {
-            float ext = chi[a] - clo[a];
-            if (!(ext > 0.0f)) continue;
-            float bl[kBins][3], bh[kBins][3];
-            uint32_t bc[kBins] = {};
-            for (int b = 0; b < kBins; ++b)
-                for (int j = 0; j < 3; ++j) { bl[b][j] = INFINITY; bh[b][j] = -INFINITY; }
-            float k = (float)kBins / ext;
-            for (uint32_t i = first; i < first + count; ++i) {
-                const Prim &p = prims[idx[i]];
-                int b = std::min(kBins - 1, (int)((p.c[a] - clo[a]) * k));
-                ++bc[b];
-                for (int j = 0; j < 3; ++j) { bl[b][j] = std::min(bl[b][j], p.lo[j]); bh[b][j] = std::max(bh[b][j], p.hi[j]); }
-            }
+            if (!use[a]) continue;
+            auto &bl = all->bl[a];
+            auto &bh = all->bh[a];
+            auto &bc = all->bc[a];
             float rarea[kBins];
             uint32_t rcount[kBins];
             float rl[3] = {INFINITY, INFINITY, INFINITY}, rh[3] = {-INFINITY, -INFINITY, -INFINITY};
@@ -427,11 +522,46 @@ struct Builder {
             if (count <= kMaxLeaf && leaf_cost <= split_cost) return leaf(first, count, lo, hi);
             float ext = chi[best_axis] - clo[best_axis];
             float k = (float)kBins / ext;
-            auto it = std::partition(idx.begin() + first, idx.begin() + first + count, [&](uint32_t i) {
+            auto left = [&](uint32_t i) {
                 int b = std::min(kBins - 1, (int)((prims[i].c[best_axis] - clo[best_axis]) * k));
                 return b <= best_bin;
-            });
-            mid = (uint32_t)(it - idx.begin());
+            };
+            if (wide > 1) {
+                // stable partition by chunks: count, place through a scratch array, copy back
+                std::vector<uint32_t> lefts(wide, 0), starts(wide, 0);
+                par_chunks(first, count, wide, [&](uint32_t b, uint32_t e, unsigned t) {
+                    uint32_t n = 0;
+                    for (uint32_t i = b; i < e; ++i) n += left(idx[i]) ? 1u : 0u;
+                    lefts[t] = n;
+                    starts[t] = b;
+                });
+                uint32_t total_left = 0;
+                std::vector<uint32_t> lpos(wide), rpos(wide);
+                for (unsigned t = 0; t < wide; ++t) {
+                    lpos[t] = total_left;
+                    total_left += lefts[t];
+                }
+                uint32_t r_at = total_left;
+                for (unsigned t = 0; t < wide; ++t) {
+                    rpos[t] = r_at;
+                    uint32_t chunk = (t + 1 < wide ? starts[t + 1] : first + count) - starts[t];
+                    r_at += chunk - lefts[t];
+                }
+                std::vector<uint32_t> tmp(count);
+                par_chunks(first, count, wide, [&](uint32_t b, uint32_t e, unsigned t) {
+                    uint32_t l = lpos[t], r = rpos[t];
+                    for (uint32_t i = b; i < e; ++i) {
+                        uint32_t v = idx[i];
+                        if (left(v)) tmp[l++] = v;
+                        else tmp[r++] = v;
+                    }
+                });
+                std::copy(tmp.begin(), tmp.end(), idx.begin() + first);
+                mid = first + total_left;
+            } else {
+                auto it = std::partition(idx.begin() + first, idx.begin() + first + count, left);
+                mid = (uint32_t)(it - idx.begin());
+            }
             if (mid == first || mid == first + count) mid = first + count / 2;
         }
         size_t node = nodes.size();
@@ -489,20 +619,24 @@ void build_bvh(HostScene &s) {
     Builder b;
     b.prims.resize(n);
     std::vector<f3> v(n * 3);
-    for (size_t i = 0; i < n; ++i) {
-        const dl_mesh &m = *s.meshes[s.occ_mesh[i]];
-        Prim &p = b.prims[i];
-        for (int k = 0; k < 3; ++k) {
-            const float *q = m.positions + (size_t)m.indices[(size_t)s.occ_tri[i] * 3 + k] * 3;
-            v[i * 3 + k] = f3{q[0], q[1], q[2]};
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned wide = n > kWidePrims ? hw : 1u;
+    par_chunks(0, (uint32_t)n, wide, [&](uint32_t lo_i, uint32_t hi_i, unsigned) {
+        for (size_t i = lo_i; i < hi_i; ++i) {
+            const dl_mesh &m = *s.meshes[s.occ_mesh[i]];
+            Prim &p = b.prims[i];
+            for (int k = 0; k < 3; ++k) {
+                const float *q = m.positions + (size_t)m.indices[(size_t)s.occ_tri[i] * 3 + k] * 3;
+                v[i * 3 + k] = f3{q[0], q[1], q[2]};
+            }
+            for (int a = 0; a < 3; ++a) {
+                float x0 = axis_of(v[i * 3], a), x1 = axis_of(v[i * 3 + 1], a), x2 = axis_of(v[i * 3 + 2], a);
+                p.lo[a] = std::min(x0, std::min(x1, x2));
+                p.hi[a] = std::max(x0, std::max(x1, x2));
+                p.c[a] = (p.lo[a] + p.hi[a]) * 0.5f;
+            }
         }
-        for (int a = 0; a < 3; ++a) {
-            float x0 = axis_of(v[i * 3], a), x1 = axis_of(v[i * 3 + 1], a), x2 = axis_of(v[i * 3 + 2], a);
-            p.lo[a] = std::min(x0, std::min(x1, x2));
-            p.hi[a] = std::max(x0, std::max(x1, x2));
-            p.c[a] = (p.lo[a] + p.hi[a]) * 0.5f;
-        }
-    }
+    });
     b.idx.resize(n);
     std::iota(b.idx.begin(), b.idx.end(), 0u);
     std::vector<BvhNode> nodes;
@@ -539,17 +673,19 @@ void build_bvh(HostScene &s) {
     }
     s.nodes = std::move(nodes);
     s.bvh_depth = max_depth;
-    for (size_t k = 0; k < n; ++k) {
-        uint32_t i = b.idx[k];
-        f3 a = v[i * 3], e1 = sub(v[i * 3 + 1], a), e2 = sub(v[i * 3 + 2], a);
-        uint32_t bits = i;
-        float w;
-        std::memcpy(&w, &bits, 4);
-        float *p0 = &s.tri_v0[k * 4], *p1 = &s.tri_e1[k * 4], *p2 = &s.tri_e2[k * 4];
-        p0[0] = a.x; p0[1] = a.y; p0[2] = a.z; p0[3] = w;
-        p1[0] = e1.x; p1[1] = e1.y; p1[2] = e1.z; p1[3] = 0.0f;
-        p2[0] = e2.x; p2[1] = e2.y; p2[2] = e2.z; p2[3] = 0.0f;
-    }
+    par_chunks(0, (uint32_t)n, wide, [&](uint32_t lo_k, uint32_t hi_k, unsigned) {
+        for (size_t k = lo_k; k < hi_k; ++k) {
+            uint32_t i = b.idx[k];
+            f3 a = v[i * 3], e1 = sub(v[i * 3 + 1], a), e2 = sub(v[i * 3 + 2], a);
+            uint32_t bits = i;
+            float w;
+            std::memcpy(&w, &bits, 4);
+            float *p0 = &s.tri_v0[k * 4], *p1 = &s.tri_e1[k * 4], *p2 = &s.tri_e2[k * 4];
+            p0[0] = a.x; p0[1] = a.y; p0[2] = a.z; p0[3] = w;
+            p1[0] = e1.x; p1[1] = e1.y; p1[2] = e1.z; p1[3] = 0.0f;
+            p2[0] = e2.x; p2[1] = e2.y; p2[2] = e2.z; p2[3] = 0.0f;
+        }
+    });
 }
 
 // ---- payload (src/bake/format/mod.rs:170-213, lights.rs:27-52, maps.rs:16-37) -------------------
