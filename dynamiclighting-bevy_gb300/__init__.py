@@ -411,6 +411,8 @@ def load_library(path: str = LIBRARY_PATH):
     lib.dl_encode_payload.argtypes = [P(DlBakedScene), P(P(C.c_uint8)), P(C.c_uint64),
                                       P(C.c_uint32)]
     lib.dl_free.argtypes = [C.c_void_p]
+    lib.dl_session_encode_payload.restype = C.c_int
+    lib.dl_session_encode_payload.argtypes = [C.c_void_p, P(P(C.c_uint8)), P(C.c_uint64), P(C.c_uint32)]
     lib.dl_session_bounce_map.restype = C.c_int
     lib.dl_session_bounce_map.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_void_p, C.c_void_p,
                                           C.c_uint32, P(C.c_uint32)]
@@ -488,6 +490,20 @@ class Session:
         r = DlBakeReport()
         self.lib.dl_session_report(self.handle, C.byref(r))
         return r
+
+    def encode_payload(self) -> tuple:
+        """The last run's .dynlight payload built on the device and its CRC-32
+        (dl_session_encode_payload)."""
+        data = C.POINTER(C.c_uint8)()
+        length = C.c_uint64()
+        crc = C.c_uint32()
+        status = self.lib.dl_session_encode_payload(self.handle, C.byref(data), C.byref(length), C.byref(crc))
+        if status != 0:
+            _raise(self.lib, status)
+        try:
+            return bytes(np.ctypeslib.as_array(data, shape=(length.value,))), crc.value
+        finally:
+            self.lib.dl_free(data)
 
     def bounce_map(self, mesh_id: int, slot: int):
         """The last run's filtered bounce map of (mesh id, light slot) before quantization:

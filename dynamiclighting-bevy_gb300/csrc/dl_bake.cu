@@ -1187,6 +1187,21 @@ __device__ __forceinline__ uint32_t crop_level(const uint32_t *pool, uint32_t of
 
 constexpr int kCropBytes = 2048;  // per-warp staging grid in shared memory (texels)
 
+// 1-bit words LSB first (bits.rs:40-46): word w holds texels 32w .. 32w + 31, so lane j's texel of
+// word w is bit j of a warp ballot. Each round of 32 words ends with one coalesced store per lane.
+template <class Texel>
+__device__ __forceinline__ void ballot_words(uint64_t n, uint64_t nw, uint32_t *out, unsigned lane, Texel texel) {
+    for (uint64_t base = 0; base < nw; base += 32) {
+        uint32_t mine = 0;
+        for (uint32_t k = 0; k < 32 && base + k < nw; ++k) {
+            uint64_t i = (base + k) * 32 + lane;
+            uint32_t b = __ballot_sync(0xFFFFFFFFu, i < n && texel(i) != 0);
+            if (lane == k) mine = b;
+        }
+        if (base + lane < nw) out[base + lane] = mine;
+    }
+}
+
 __global__ void __launch_bounds__(kBlock) k_crop(DevScene sc, uint32_t entries, const uint32_t *entry_pair,
                                                 const unsigned long long *entry_dst, const uint32_t *pair_tri,
                                                 const uint32_t *pair_light, const uint4 *tri_crop,
@@ -1212,6 +1227,12 @@ __global__ void __launch_bounds__(kBlock) k_crop(DevScene sc, uint32_t entries, 
     unsigned long long dst = entry_dst[e];
     if (n > (uint64_t)kCropBytes) {
         // large crops: every texel straight from the region
+        if (bits == 1) {
+            ballot_words(n, nw, words + dst, lane, [&](uint64_t i) {
+                return crop_level(region_pool, off, r, bits, c, gw, gh, (int)(i % gw), (int)(i / gw));
+            });
+            return;
+        }
         for (uint64_t wi = lane; wi < nw; wi += 32) {
             uint32_t word = 0;
             for (uint32_t j = 0; j < per; ++j) {
@@ -1259,15 +1280,74 @@ __global__ void __launch_bounds__(kBlock) k_crop(DevScene sc, uint32_t entries, 
         g[i] = (uint8_t)v;
     }
     __syncwarp();
+    if (bits == 1) {
+        ballot_words(n, nw, words + dst, lane, [&](uint64_t i) { return (uint32_t)g[i]; });
+        return;
+    }
     for (uint64_t wi = lane; wi < nw; wi += 32) {
         uint32_t word = 0;
         for (uint32_t j = 0; j < per; ++j) {
             uint64_t i = wi * per + j;
             if (i >= n) break;
-            uint32_t v = g[i];
-            word |= (bits == 1 ? (v != 0) : v) << (j * bits);
+            word |= (uint32_t)g[i] << (j * bits);
         }
         words[dst + wi] = word;
+    }
+}
+
+// ================================ payload on the device ====================================
+// The .dynlight payload assembled next to the resident words and its CRC-32 computed there, so
+// the host receives finished bytes (src/bake/format/mod.rs:101-119,170-213).
+
+// One piece of the payload: `len` words from `src` (device memory) to payload word `dst`.
+struct PayloadSegment {
+    unsigned long long dst;
+    const uint32_t *src;
+    unsigned long long len;
+};
+__global__ void k_payload_gather(const PayloadSegment *seg, uint32_t *out) {
+    PayloadSegment g = seg[blockIdx.x];
+    for (unsigned long long i = threadIdx.x; i < g.len; i += blockDim.x) out[g.dst + i] = g.src[i];
+}
+
+constexpr uint32_t kCrcChunkWords = 16384;  // 64 KiB chunks, 128 threads x 512 bytes
+struct CrcShifts {
+    uint32_t m[7][32];  // shift of the CRC register by 512 * 2^l bytes, l = 0 .. 6, as GF(2) columns
+};
+__device__ __forceinline__ uint32_t gf2_times(const uint32_t *m, uint32_t v) {
+    uint32_t r = 0;
+    for (int i = 0; i < 32; ++i)
+        if ((v >> i) & 1u) r ^= m[i];
+    return r;
+}
+// The raw CRC-32 register (from zero, no inversion) of every full 64 KiB chunk: each of 128
+// threads runs 512 bytes by slicing by 4 over little-endian words (Kounavis & Berry 2008), then
+// the block combines the parts pairwise, raw(A B) = shift(raw(A), |B|) ^ raw(B).
+__global__ void __launch_bounds__(128) k_crc_chunks(const uint32_t *data, unsigned long long chunks,
+                                                    const uint32_t *tables, CrcShifts sh, uint32_t *out) {
+    __shared__ uint32_t t[4][256];
+    __shared__ uint32_t part[128];
+    __shared__ uint32_t m[7][32];
+    for (int i = threadIdx.x; i < 1024; i += 128) t[i / 256][i % 256] = tables[i];
+    for (int i = threadIdx.x; i < 224; i += 128) m[i / 32][i % 32] = sh.m[i / 32][i % 32];
+    __syncthreads();
+    for (unsigned long long chunk = blockIdx.x; chunk < chunks; chunk += gridDim.x) {
+        const uint32_t *p = data + chunk * kCrcChunkWords + threadIdx.x * 128;
+        uint32_t c = 0;
+        for (int i = 0; i < 128; ++i) {
+            c ^= p[i];
+            c = t[3][c & 0xFF] ^ t[2][(c >> 8) & 0xFF] ^ t[1][(c >> 16) & 0xFF] ^ t[0][c >> 24];
+        }
+        part[threadIdx.x] = c;
+        __syncthreads();
+        for (int l = 0; l < 7; ++l) {
+            unsigned stride = 1u << l;
+            if ((threadIdx.x & (2 * stride - 1)) == 0)
+                part[threadIdx.x] = gf2_times(m[l], part[threadIdx.x]) ^ part[threadIdx.x + stride];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[chunk] = part[0];
+        __syncthreads();
     }
 }
 
@@ -2352,13 +2432,60 @@ dl_status run(dl_session &s, dl_progress *progress) {
     return DL_OK;
 }
 
+// Host buffers of freed results' words, handed to the next result so that its download writes
+// pages that are already mapped (a fresh buffer of this size spends most of its copy time in
+// first-touch page faults). At most kCacheBytes are held.
+struct WordCache {
+    static constexpr size_t kCacheBytes = size_t(2) << 30;
+    std::mutex lock;
+    std::vector<std::pair<size_t, uint32_t *>> free;  // (capacity in words, buffer)
+    size_t held = 0;
+    uint32_t *take(size_t n, size_t &cap) {
+        std::lock_guard<std::mutex> guard(lock);
+        size_t best = free.size();
+        for (size_t i = 0; i < free.size(); ++i)
+            if (free[i].first >= n && (best == free.size() || free[i].first < free[best].first)) best = i;
+        if (best < free.size()) {
+            auto e = free[best];
+            free.erase(free.begin() + best);
+            held -= e.first * 4;
+            cap = e.first;
+            return e.second;
+        }
+        cap = n;
+        return new uint32_t[n ? n : 1];
+    }
+    void give(uint32_t *p, size_t cap) {
+        std::lock_guard<std::mutex> guard(lock);
+        while (held + cap * 4 > kCacheBytes && !free.empty()) {  // drop the oldest
+            held -= free.front().first * 4;
+            delete[] free.front().second;
+            free.erase(free.begin());
+        }
+        if (cap * 4 > kCacheBytes) {
+            delete[] p;
+            return;
+        }
+        free.emplace_back(cap, p);
+        held += cap * 4;
+    }
+};
+WordCache &word_cache() {
+    static WordCache *c = new WordCache;  // never destroyed: results may be freed during exit
+    return *c;
+}
+
 // The result in one host allocation: the scene struct, its arrays, then the words.
 struct HostResult {
     dl_baked_scene scene;
     std::vector<dl_baked_light> lights;
     std::vector<dl_light_bvh_node> bvh;
     std::vector<dl_baked_mesh> meshes;
-    std::vector<uint32_t> words;
+    uint32_t *words = nullptr;  // from word_cache(), `words_cap` words
+    size_t words_cap = 0;
+    ~HostResult() {
+        if (words) word_cache().give(words, words_cap);
+    }
     std::vector<uint32_t> cubes;
     std::vector<std::vector<uint32_t>> sun_words;
     std::vector<dl_sun_map> sun_maps;
@@ -2366,17 +2493,23 @@ struct HostResult {
     dl_sky_probes probes{};
 };
 
-dl_status result(dl_session &s, dl_baked_scene *&out) {
+// The last run's scene. With `download` false the triangle words, distance cubes and sun map
+// texels stay on the device and the scene's pointers to them are device pointers (for the
+// device-side payload encode); everything else is on the host either way.
+dl_status assemble(dl_session &s, std::unique_ptr<HostResult> &r, bool download) {
     if (!s.have_result) {
         g_error = "no finished run in this session";
         return DL_INVALID_ARGUMENT;
     }
-    auto r = std::make_unique<HostResult>();
+    r = std::make_unique<HostResult>();
     const HostScene &h = s.host;
-    r->words.resize(s.out_words);
-    if (s.out_words)
-        CK(cudaMemcpy(r->words.data(), s.words_dev, s.out_words * 4, cudaMemcpyDeviceToHost));
-    s.report.d2h_bytes = s.out_words * 4 + (s.mesh_words.size() * 8) + sizeof(Counters);
+    const uint32_t *words = s.words_dev;
+    if (download) {
+        r->words = word_cache().take(s.out_words, r->words_cap);
+        if (s.out_words) CK(cudaMemcpy(r->words, s.words_dev, s.out_words * 4, cudaMemcpyDeviceToHost));
+        words = r->words;
+        s.report.d2h_bytes = s.out_words * 4 + (s.mesh_words.size() * 8) + sizeof(Counters);
+    }
     uint64_t at = 0;
     for (uint32_t m = 0; m < h.meshes.size(); ++m) {
         const dl_mesh &mm = *h.meshes[m];
@@ -2385,7 +2518,7 @@ dl_status result(dl_session &s, dl_baked_scene *&out) {
         b.content_hash = mm.content_hash;
         b.resolution = h.resolution[m];
         b.occludes = mm.occludes ? 1 : 0;
-        b.triangles = r->words.data() + at;
+        b.triangles = words + at;
         b.word_count = s.mesh_words[m];
         at += s.mesh_words[m];
         r->meshes.push_back(b);
@@ -2427,29 +2560,41 @@ dl_status result(dl_session &s, dl_baked_scene *&out) {
     sc.mesh_count = r->meshes.size();
     sc.meshes = r->meshes.data();
     // maps for moving meshes
-    if (s.cube_word_count) {
+    if (s.cube_word_count && download) {
         r->cubes.resize(s.cube_word_count);
         CK(cudaMemcpy(r->cubes.data(), s.cube_words, s.cube_word_count * 4, cudaMemcpyDeviceToHost));
     }
+    std::vector<const uint32_t *> sun_dev;
     for (size_t i = 0; i < s.sun_setups.size(); ++i) {
         const SunMapSetup &m = s.sun_setups[i];
         dl_sun_map d{};
         std::vector<uint32_t> texels;
+        const uint32_t *dev = nullptr;
         if (m.empty) {
             texels.assign(1, 0xFFFFFFFFu);  // pack_sun_depth(1, 1)
             d.resolution = 1;
         } else {
-            texels.resize(((uint64_t)m.resolution * m.resolution + 1) / 2);
-            CK(cudaMemcpy(texels.data(), s.sun_texels[i], texels.size() * 4, cudaMemcpyDeviceToHost));
             d.resolution = m.resolution;
             for (int k = 0; k < 12; ++k) d.rows[k] = m.rows[k];
+            d.word_count = ((uint64_t)m.resolution * m.resolution + 1) / 2;
+            if (download) {
+                texels.resize(d.word_count);
+                CK(cudaMemcpy(texels.data(), s.sun_texels[i], texels.size() * 4, cudaMemcpyDeviceToHost));
+            } else {
+                dev = s.sun_texels[i];
+            }
         }
         r->sun_words.push_back(std::move(texels));
         r->sun_maps.push_back(d);
+        sun_dev.push_back(dev);
     }
     for (size_t i = 0; i < r->sun_maps.size(); ++i) {
-        r->sun_maps[i].word_count = r->sun_words[i].size();
-        r->sun_maps[i].texels = r->sun_words[i].data();
+        if (sun_dev[i]) {
+            r->sun_maps[i].texels = sun_dev[i];
+        } else {
+            r->sun_maps[i].word_count = r->sun_words[i].size();
+            r->sun_maps[i].texels = r->sun_words[i].data();
+        }
     }
     if (s.probe_grid.present) {
         const ProbeGridSetup &g = s.probe_grid;
@@ -2467,10 +2612,15 @@ dl_status result(dl_session &s, dl_baked_scene *&out) {
         p.word_count = r->probe_words.size();
         p.words = r->probe_words.data();
     }
-    for (const auto &w : r->sun_words) s.report.d2h_bytes += w.size() * 4;
-    s.report.d2h_bytes += r->cubes.size() * 4 + (s.probe_grid.present ? s.probe_grid.count() * 6 * 8 : 0);
-    sc.distance_cube_words = r->cubes.size();
-    sc.distance_cubes = r->cubes.empty() ? nullptr : r->cubes.data();
+    if (download) {
+        for (const auto &w : r->sun_words) s.report.d2h_bytes += w.size() * 4;
+        s.report.d2h_bytes += r->cubes.size() * 4 + (s.probe_grid.present ? s.probe_grid.count() * 6 * 8 : 0);
+        sc.distance_cube_words = r->cubes.size();
+        sc.distance_cubes = r->cubes.empty() ? nullptr : r->cubes.data();
+    } else {
+        sc.distance_cube_words = s.cube_word_count;
+        sc.distance_cubes = s.cube_words;
+    }
     sc.sun_map_count = r->sun_maps.size();
     sc.sun_maps = r->sun_maps.empty() ? nullptr : r->sun_maps.data();
     sc.sky_probes = s.probe_grid.present ? &r->probes : nullptr;
@@ -2481,6 +2631,110 @@ dl_status result(dl_session &s, dl_baked_scene *&out) {
     sc.stats.lights_removed = s.counters.lights_removed;
     sc.stats.bounce_rays = s.counters.bounce_rays;
     sc.stats.triangle_words = s.out_words;
+    return DL_OK;
+}
+
+// Collects the payload as host-written runs and device word arrays (payload order, word units).
+struct DeviceSink {
+    std::vector<uint32_t> host;         // host-written words, in order
+    std::vector<PayloadSegment> segs;   // src of a host run: offset into `host` until uploaded
+    std::vector<bool> from_host;
+    unsigned long long at = 0;          // payload words so far
+    void run(uint32_t v) {
+        if (segs.empty() || !from_host.back() || segs.back().dst + segs.back().len != at) {
+            segs.push_back(PayloadSegment{at, reinterpret_cast<const uint32_t *>(host.size()), 0});
+            from_host.push_back(true);
+        }
+        host.push_back(v);
+        ++segs.back().len;
+        ++at;
+    }
+    void u32(uint32_t v) { run(v); }
+    void u64(uint64_t v) {
+        run((uint32_t)v);
+        run((uint32_t)(v >> 32));
+    }
+    void f32(float f) {
+        uint32_t v;
+        std::memcpy(&v, &f, 4);
+        run(v);
+    }
+    void words(const uint32_t *w, uint64_t n) {
+        u64(n);
+        if (!n) return;
+        cudaPointerAttributes attr{};
+        bool device = cudaPointerGetAttributes(&attr, w) == cudaSuccess && attr.type == cudaMemoryTypeDevice;
+        cudaGetLastError();  // a host pointer may leave an error behind on older drivers
+        if (!device) {
+            for (uint64_t i = 0; i < n; ++i) run(w[i]);
+            return;
+        }
+        segs.push_back(PayloadSegment{at, w, n});
+        from_host.push_back(false);
+        at += n;
+    }
+};
+
+// dl_session_encode_payload: the payload of the last run built on the device, its CRC-32 from
+// per-chunk CRCs combined on the host.
+dl_status encode_device(dl_session &s, uint8_t *&bytes, uint64_t &length, uint32_t &crc) {
+    std::unique_ptr<HostResult> r;
+    dl_status st = assemble(s, r, false);
+    if (st != DL_OK) return st;
+    DeviceSink sink;
+    emit_payload(r->scene, sink);
+    const unsigned long long words = sink.at;
+    Pool &P = s.pool;
+    cudaStream_t strm = s.stream;
+    uint32_t *payload = P.get<uint32_t>("payload", words);
+    uint32_t *host_dev = P.get<uint32_t>("payload_host", sink.host.size());
+    CK(cudaMemcpyAsync(host_dev, sink.host.data(), sink.host.size() * 4, cudaMemcpyHostToDevice, strm));
+    for (size_t i = 0; i < sink.segs.size(); ++i)
+        if (sink.from_host[i]) sink.segs[i].src = host_dev + reinterpret_cast<uintptr_t>(sink.segs[i].src);
+    PayloadSegment *segs = P.get<PayloadSegment>("payload_segs", sink.segs.size());
+    CK(cudaMemcpyAsync(segs, sink.segs.data(), sink.segs.size() * sizeof(PayloadSegment), cudaMemcpyHostToDevice,
+                       strm));
+    k_payload_gather<<<(unsigned)sink.segs.size(), 256, 0, strm>>>(segs, payload);
+    LAUNCHED("k_payload_gather");
+    // CRC of the full chunks on the device
+    const unsigned long long chunks = words / kCrcChunkWords;
+    std::vector<uint32_t> chunk_crc(chunks);
+    if (chunks) {
+        uint32_t *tables = P.get<uint32_t>("crc_tables", 1024);
+        CK(cudaMemcpyAsync(tables, crc32_tables(), 1024 * 4, cudaMemcpyHostToDevice, strm));
+        CrcShifts sh{};
+        for (int l = 0; l < 7; ++l)
+            for (int i = 0; i < 32; ++i) sh.m[l][i] = crc32_shift(1u << i, 512ull << l);
+        uint32_t *out = P.get<uint32_t>("chunk_crc", chunks);
+        unsigned blocks = (unsigned)std::min<unsigned long long>(chunks, (unsigned long long)s.sms * 16);
+        k_crc_chunks<<<blocks, 128, 0, strm>>>(payload, chunks, tables, sh, out);
+        LAUNCHED("k_crc_chunks");
+        CK(cudaMemcpyAsync(chunk_crc.data(), out, chunks * 4, cudaMemcpyDeviceToHost, strm));
+    }
+    length = words * 4;
+    bytes = static_cast<uint8_t *>(std::malloc(length ? length : 1));
+    if (!bytes) throw std::bad_alloc();
+    CK(cudaMemcpyAsync(bytes, payload, length, cudaMemcpyDeviceToHost, strm));
+    CK(cudaStreamSynchronize(strm));
+    uint32_t shift64[32];
+    for (int i = 0; i < 32; ++i) shift64[i] = crc32_shift(1u << i, (uint64_t)kCrcChunkWords * 4);
+    uint32_t c = 0xFFFFFFFFu;
+    for (unsigned long long k = 0; k < chunks; ++k) {
+        uint32_t shifted = 0;
+        for (int i = 0; i < 32; ++i)
+            if ((c >> i) & 1u) shifted ^= shift64[i];
+        c = shifted ^ chunk_crc[k];
+    }
+    uint64_t done = chunks * (uint64_t)kCrcChunkWords * 4;
+    c = crc32_update(c, bytes + done, length - done);
+    crc = c ^ 0xFFFFFFFFu;
+    return DL_OK;
+}
+
+dl_status result(dl_session &s, dl_baked_scene *&out) {
+    std::unique_ptr<HostResult> r;
+    dl_status st = assemble(s, r, true);
+    if (st != DL_OK) return st;
     out = &r.release()->scene;
     return DL_OK;
 }
@@ -2633,6 +2887,30 @@ dl_status dl_session_bounce_map(dl_session *s, uint64_t mesh_id, uint32_t slot, 
                 rgb[k * 3 + 2] = v[k].z;
             }
         }
+        return DL_OK;
+    })
+}
+
+dl_status dl_session_encode_payload(dl_session *s, uint8_t **bytes, uint64_t *length, uint32_t *crc) {
+    if (!s || !bytes || !length) {
+        g_error = "null argument";
+        return DL_INVALID_ARGUMENT;
+    }
+    *bytes = nullptr;
+    *length = 0;
+    DL_GUARD({
+        CK(cudaSetDevice(s->device));
+        uint8_t *b = nullptr;
+        uint64_t n = 0;
+        uint32_t c = 0;
+        dl_status st = encode_device(*s, b, n, c);
+        if (st != DL_OK) {
+            std::free(b);
+            return st;
+        }
+        *bytes = b;
+        *length = n;
+        if (crc) *crc = c;
         return DL_OK;
     })
 }

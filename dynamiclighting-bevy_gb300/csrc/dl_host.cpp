@@ -695,7 +695,19 @@ struct Writer {
     void u32(uint32_t v) { for (int i = 0; i < 4; ++i) b.push_back((uint8_t)(v >> (8 * i))); }
     void u64(uint64_t v) { for (int i = 0; i < 8; ++i) b.push_back((uint8_t)(v >> (8 * i))); }
     void f32(float f) { uint32_t v; std::memcpy(&v, &f, 4); u32(v); }
-    void words(const uint32_t *w, uint64_t n) { u64(n); for (uint64_t i = 0; i < n; ++i) u32(w[i]); }
+    void words(const uint32_t *w, uint64_t n) {
+        u64(n);
+        size_t at = b.size();
+        b.resize(at + n * 4);
+        for (uint64_t i = 0; i < n; ++i) {  // little-endian words, whatever the host's order
+            uint32_t v = w[i];
+            uint8_t *o = &b[at + i * 4];
+            o[0] = (uint8_t)v;
+            o[1] = (uint8_t)(v >> 8);
+            o[2] = (uint8_t)(v >> 16);
+            o[3] = (uint8_t)(v >> 24);
+        }
+    }
 };
 }  // namespace
 
@@ -835,75 +847,77 @@ std::vector<uint32_t> sky_probe_words(const ProbeGridSetup &g, const float *open
 
 std::vector<uint8_t> encode_payload(const dl_baked_scene &s) {
     Writer w;
-    w.u32((s.settings.bounce ? 1u : 0u) | (s.settings.colored_bounce ? 2u : 0u));
-    w.u32(s.settings.dynamic_geometry);
-    w.f32(s.settings.pixel_density);
-    w.u32(s.settings.max_lightmap_size);
-    w.u32(s.settings.distance_cube_resolution);
-    w.u64(s.light_count);
-    for (uint64_t i = 0; i < s.light_count; ++i) {
-        const dl_baked_light &l = s.lights[i];
-        w.u64(l.id);
-        for (int k = 0; k < 3; ++k) w.f32(l.origin[k]);
-        w.f32(l.radius);
-        w.u32(l.bounce_bits);
-        w.u32(l.shape);
-        for (int k = 0; k < 4; ++k) w.f32(l.rotation[k]);
-        for (int k = 0; k < 2; ++k) w.f32(l.size[k]);
-        w.u32(l.shadow_bits_per_texel);
-    }
-    w.words(reinterpret_cast<const uint32_t *>(s.light_bvh), s.light_bvh_count * 8);
-    w.u64(s.mesh_count);
-    for (uint64_t i = 0; i < s.mesh_count; ++i) {
-        const dl_baked_mesh &m = s.meshes[i];
-        w.u64(m.id);
-        w.u64(m.content_hash);
-        w.u32(m.resolution);
-        w.u32(m.occludes ? 1u : 0u);
-        w.words(m.triangles, m.word_count);
-    }
-    w.words(s.distance_cubes, s.distance_cube_words);
-    // maps::encode (format/maps.rs:16-38)
-    w.u64(s.sun_map_count);
-    for (uint64_t i = 0; i < s.sun_map_count; ++i) {
-        const dl_sun_map &m = s.sun_maps[i];
-        w.u32(m.resolution);
-        for (float r : m.rows) w.f32(r);
-        w.words(m.texels, m.word_count);
-    }
-    w.u32(s.sky_probes ? 1u : 0u);
-    if (s.sky_probes) {
-        const dl_sky_probes &p = *s.sky_probes;
-        for (float v : p.origin) w.f32(v);
-        w.f32(p.spacing);
-        for (uint32_t c : p.counts) w.u32(c);
-        w.words(p.words, p.word_count);
-    }
-    w.u32(s.stats.meshes);
-    w.u64(s.stats.triangles);
-    w.u64(s.stats.texels);
-    w.u64(s.stats.rays);
-    w.u64(s.stats.lights_removed);
-    w.u64(s.stats.bounce_rays);
-    w.u64(s.stats.triangle_words);
+    emit_payload(s, w);
     return w.b;
 }
 
 // CRC-32 (IEEE 802.3, reflected polynomial 0xEDB88320), table-driven.
-uint32_t crc32_ieee(const uint8_t *data, size_t n) {
-    static uint32_t table[256];
-    static bool ready = false;
-    if (!ready) {
+// CRC-32 tables for slicing by 8 (Intel's slicing-by-8, Kounavis & Berry 2008): t[0] is the
+// byte-at-a-time table of the reflected polynomial 0xEDB88320, t[k] advances k more zero bytes.
+struct Crc32Tables {
+    uint32_t t[8][256];
+    Crc32Tables() {
         for (uint32_t i = 0; i < 256; ++i) {
             uint32_t c = i;
             for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
-            table[i] = c;
+            t[0][i] = c;
         }
-        ready = true;
+        for (uint32_t i = 0; i < 256; ++i)
+            for (int k = 1; k < 8; ++k) t[k][i] = t[0][t[k - 1][i] & 0xFF] ^ (t[k - 1][i] >> 8);
     }
-    uint32_t c = 0xFFFFFFFFu;
-    for (size_t i = 0; i < n; ++i) c = table[(c ^ data[i]) & 0xFF] ^ (c >> 8);
-    return c ^ 0xFFFFFFFFu;
+};
+const Crc32Tables &crc_tables() {
+    static const Crc32Tables tables;
+    return tables;
+}
+const uint32_t *crc32_tables() { return &crc_tables().t[0][0]; }
+
+uint32_t crc32_update(uint32_t c, const uint8_t *data, size_t n) {
+    const auto &t = crc_tables().t;
+    size_t i = 0;
+    for (; i + 8 <= n; i += 8) {
+        uint32_t lo = c ^ ((uint32_t)data[i] | (uint32_t)data[i + 1] << 8 | (uint32_t)data[i + 2] << 16 |
+                           (uint32_t)data[i + 3] << 24);
+        uint32_t hi = (uint32_t)data[i + 4] | (uint32_t)data[i + 5] << 8 | (uint32_t)data[i + 6] << 16 |
+                      (uint32_t)data[i + 7] << 24;
+        c = t[7][lo & 0xFF] ^ t[6][(lo >> 8) & 0xFF] ^ t[5][(lo >> 16) & 0xFF] ^ t[4][lo >> 24] ^ t[3][hi & 0xFF] ^
+            t[2][(hi >> 8) & 0xFF] ^ t[1][(hi >> 16) & 0xFF] ^ t[0][hi >> 24];
+    }
+    for (; i < n; ++i) c = t[0][(c ^ data[i]) & 0xFF] ^ (c >> 8);
+    return c;
+}
+
+uint32_t crc32_ieee(const uint8_t *data, size_t n) { return crc32_update(0xFFFFFFFFu, data, n) ^ 0xFFFFFFFFu; }
+
+// The CRC register after `n` more zero bytes: multiplication by x^(8n) modulo the polynomial,
+// by squaring the one-zero-byte operator (the technique of zlib's crc32_combine).
+namespace {
+uint32_t gf2_times(const uint32_t m[32], uint32_t v) {
+    uint32_t r = 0;
+    for (int i = 0; v; ++i, v >>= 1)
+        if (v & 1) r ^= m[i];
+    return r;
+}
+void gf2_square(uint32_t out[32], const uint32_t m[32]) {
+    for (int i = 0; i < 32; ++i) out[i] = gf2_times(m, m[i]);
+}
+}  // namespace
+uint32_t crc32_shift(uint32_t c, uint64_t n) {
+    uint32_t odd[32], even[32];
+    odd[0] = 0xEDB88320u;  // the operator for one zero bit
+    for (int i = 1; i < 32; ++i) odd[i] = 1u << (i - 1);
+    gf2_square(even, odd);  // two zero bits
+    gf2_square(odd, even);  // four zero bits
+    while (n) {
+        gf2_square(even, odd);  // 8, 32, 128, ... zero bits: one byte, then 4, 16, ... bytes
+        if (n & 1) c = gf2_times(even, c);
+        n >>= 1;
+        if (!n) break;
+        gf2_square(odd, even);  // 2, 8, 32, ... bytes
+        if (n & 1) c = gf2_times(odd, c);
+        n >>= 1;
+    }
+    return c;
 }
 
 }  // namespace dl

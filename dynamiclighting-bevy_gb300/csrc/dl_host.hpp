@@ -107,8 +107,73 @@ ProbeGridSetup sky_probe_grid(const HostScene &s, float spacing);
 std::vector<uint32_t> sky_probe_words(const ProbeGridSetup &g, const float *open, const uint32_t *back,
                                       uint32_t samples);
 
-// The .dynlight payload (src/bake/format/mod.rs:170-213) and its CRC-32.
+// The .dynlight payload sections in order (src/bake/format/mod.rs:170-213, lights.rs:27-52,
+// maps.rs:16-38) into `w`, which takes little-endian u32/u64/f32 values and word arrays
+// (`words(pointer, count)` writes the count as a u64, then the words).
+template <class Sink>
+void emit_payload(const dl_baked_scene &s, Sink &w) {
+    w.u32((s.settings.bounce ? 1u : 0u) | (s.settings.colored_bounce ? 2u : 0u));
+    w.u32(s.settings.dynamic_geometry);
+    w.f32(s.settings.pixel_density);
+    w.u32(s.settings.max_lightmap_size);
+    w.u32(s.settings.distance_cube_resolution);
+    w.u64(s.light_count);
+    for (uint64_t i = 0; i < s.light_count; ++i) {
+        const dl_baked_light &l = s.lights[i];
+        w.u64(l.id);
+        for (int k = 0; k < 3; ++k) w.f32(l.origin[k]);
+        w.f32(l.radius);
+        w.u32(l.bounce_bits);
+        w.u32(l.shape);
+        for (int k = 0; k < 4; ++k) w.f32(l.rotation[k]);
+        for (int k = 0; k < 2; ++k) w.f32(l.size[k]);
+        w.u32(l.shadow_bits_per_texel);
+    }
+    w.words(reinterpret_cast<const uint32_t *>(s.light_bvh), s.light_bvh_count * 8);
+    w.u64(s.mesh_count);
+    for (uint64_t i = 0; i < s.mesh_count; ++i) {
+        const dl_baked_mesh &m = s.meshes[i];
+        w.u64(m.id);
+        w.u64(m.content_hash);
+        w.u32(m.resolution);
+        w.u32(m.occludes ? 1u : 0u);
+        w.words(m.triangles, m.word_count);
+    }
+    w.words(s.distance_cubes, s.distance_cube_words);
+    // maps::encode (format/maps.rs:16-38)
+    w.u64(s.sun_map_count);
+    for (uint64_t i = 0; i < s.sun_map_count; ++i) {
+        const dl_sun_map &m = s.sun_maps[i];
+        w.u32(m.resolution);
+        for (float r : m.rows) w.f32(r);
+        w.words(m.texels, m.word_count);
+    }
+    w.u32(s.sky_probes ? 1u : 0u);
+    if (s.sky_probes) {
+        const dl_sky_probes &p = *s.sky_probes;
+        for (float v : p.origin) w.f32(v);
+        w.f32(p.spacing);
+        for (uint32_t c : p.counts) w.u32(c);
+        w.words(p.words, p.word_count);
+    }
+    w.u32(s.stats.meshes);
+    w.u64(s.stats.triangles);
+    w.u64(s.stats.texels);
+    w.u64(s.stats.rays);
+    w.u64(s.stats.lights_removed);
+    w.u64(s.stats.bounce_rays);
+    w.u64(s.stats.triangle_words);
+}
+
+// The .dynlight payload and its CRC-32.
 std::vector<uint8_t> encode_payload(const dl_baked_scene &scene);
 uint32_t crc32_ieee(const uint8_t *data, size_t n);
+// The raw CRC-32 register (no pre- or post-inversion) after `data`, and after `n` zero bytes: with
+// them the CRC of a concatenation follows from its parts' CRCs,
+// raw(A B, c) = shift(raw(A, c), |B|) ^ raw(B, 0).
+uint32_t crc32_update(uint32_t c, const uint8_t *data, size_t n);
+// The slicing tables, 8 x 256 words: table k is the register after byte i and k zero bytes.
+const uint32_t *crc32_tables();
+uint32_t crc32_shift(uint32_t c, uint64_t n);
 
 }  // namespace dl

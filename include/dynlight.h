@@ -332,6 +332,11 @@ dl_status dl_session_run(dl_session *session, dl_progress *progress);
 /* Downloads the last run's results and serializes them. */
 dl_status dl_session_result(dl_session *session, dl_baked_scene **out);
 dl_status dl_session_report(const dl_session *session, dl_bake_report *report);
+/* encode's payload (src/bake/format/mod.rs:101-119,170-213) of the session's last run, assembled
+ * on the device next to the resident words, with its CRC-32 computed there: the same bytes as
+ * dl_encode_payload on dl_session_result's scene. `*bytes` is freed with dl_free; the gzip
+ * layer stays with the caller. */
+dl_status dl_session_encode_payload(dl_session *session, uint8_t **bytes, uint64_t *length, uint32_t *crc);
 /* No counterpart in the reference (whose BounceMap is internal to bake_mesh_bounce,
    src/bake/bounce.rs:155-217): the last run's filtered bounce map of (mesh id, light slot) —
    its window (min_x, min_y, max_x, max_y) and up to `cap` RGB texels row-major over the window,

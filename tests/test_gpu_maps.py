@@ -159,3 +159,26 @@ def test_payload_with_maps_round_trips_and_matches_the_oracle():
     finally:
         lb.oracle_free(oout)
     assert payload == want and crc == want_crc
+
+
+def test_payload_encoded_on_the_device_equals_the_host_encoding():
+    import zlib
+    # a scene whose payload spans several 64 KiB chunks, with maps, and an empty one
+    for inp, opts in (mixed_room(dl.ANGULAR),
+                      scenes.outdoor(grid=65, chunks=2, boxes=20, point_lights=3, sky_samples=16, bounce_samples=8),
+                      (dl.BakeInput([], [fx.point_light(7, (0, 1, 0), 3.0)]), fx.options())):
+        s = dl.Session(inp, opts)
+        try:
+            s.run()
+            payload, crc = s.encode_payload()
+            import ctypes as C
+            out = C.POINTER(dl._abi.DlBakedScene)()
+            assert s.lib.dl_session_result(s.handle, C.byref(out)) == 0
+            try:
+                want, want_crc = dl.encode_payload(out.contents)
+            finally:
+                s.lib.dl_baked_scene_free(out)
+        finally:
+            s.close()
+        assert payload == want
+        assert crc == want_crc == zlib.crc32(want)
