@@ -253,7 +253,7 @@ def main():
     e2e_ms = []
     e2e_rep = dl._abi.DlBakeReport()
     scene = None
-    for i in range(max(2, args.steps // 2)):
+    for i in range(max(3, args.steps // 2)):
         flush_l2(torch, flush)
         out = C.POINTER(dl._abi.DlBakedScene)()
         t0 = time.perf_counter()

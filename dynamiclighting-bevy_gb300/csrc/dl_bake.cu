@@ -1727,7 +1727,7 @@ TraceTune trace_tune(dl_session &s, TraceArgs ta, bool refine, bool count, dl_pr
     std::vector<uint32_t> grabs = c.chunk_texels ? std::vector<uint32_t>{std::max(1u, c.chunk_texels / 32)}
                                                  : std::vector<uint32_t>{1, 2};
     std::vector<uint32_t> lanes = c.sample_lanes ? std::vector<uint32_t>{c.sample_lanes}
-                                  : ta.sky_items  ? std::vector<uint32_t>{1, 4, 8}
+                                  : ta.sky_items  ? std::vector<uint32_t>{1, 4, 8, 16}
                                                   : std::vector<uint32_t>{1};
     std::vector<uint32_t> minbs = (count || refine) ? std::vector<uint32_t>{7} : std::vector<uint32_t>{7, 8};
     const uint32_t every = ta.items >= (4u << 20) ? 8 : ta.items >= (1u << 20) ? 4 : 0;
