@@ -8,13 +8,16 @@
  *
  * returns: per mesh the `dynamic_triangles` words (src/bake/triangle_words.rs:1-13), the lights
  * in light-BVH slot order (src/bake/baker.rs:41-50), the light BVH nodes
- * (src/bake/light_bvh.rs:16-22) and the bake statistics (src/bake/format/types.rs:205-222).
+ * (src/bake/light_bvh.rs:16-22), the distance cubes, sun maps and sky probes for moving meshes
+ * (src/bake/baker.rs:114-152) and the bake statistics (src/bake/format/types.rs:205-222).
  * Every struct is plain data with explicit sizes so a Rust `#[repr(C)]` mirror binds it
  * directly; no C++ or CUDA type crosses the boundary, and no exception leaves it.
  *
  * Ownership: the caller owns every input array, which is read during the call only. Results
- * live in a library allocation freed with dl_baked_scene_free(). Device memory is owned by the
- * library. One bake runs at a time per process; a second concurrent call returns DL_BUSY.
+ * live in a library allocation freed with dl_baked_scene_free(); the library keeps up to 2 GiB
+ * of freed results' word buffers to reuse for later results. Device memory is owned by the
+ * library. One dl_bake / dl_bake_ex runs at a time per process (a second concurrent call returns
+ * DL_BUSY); a dl_session is used by one thread at a time.
  */
 #ifndef DYNLIGHT_GB300_H
 #define DYNLIGHT_GB300_H
@@ -40,7 +43,8 @@ typedef enum dl_status {
     DL_OUT_OF_MEMORY = 17,  /* device or host allocation failed */
     DL_QUEUE_TIMEOUT = 18,  /* a bounded device wait gave up */
     DL_BUSY = 19,           /* another bake is running in this process */
-    DL_UNSUPPORTED = 20,    /* a requested feature this library does not bake */
+    DL_UNSUPPORTED = 20,    /* a scene this library cannot bake (a map side above 65535 texels,
+                               an occluder BVH deeper than the traversal stack) */
     DL_INVALID_ARGUMENT = 21
 } dl_status;
 

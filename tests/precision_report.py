@@ -1,6 +1,7 @@
 """Precision report of the precision-stress workload (needs a GPU; prints one JSON line).
 
     python tests/precision_report.py [--steps K] [--full-grid N]
+    python tests/precision_report.py --outdoor
 
 1. The full scene (scenes.precision_stress(): 1024x1024-vertex terrain, 200k decal quads lifted
    1e-4 m, 20k slivers of aspect up to 1e4, 256 mixed lights): device time of the bit-exact
@@ -10,6 +11,7 @@
    reference restatement (the binary32 oracle) and against the FP64 oracle, per output class
    (1-bit, 4-bit, 8-bit masks and bounce words), plus the bounce irradiance error against the
    FP64 oracle, for the refined form at epsilon 1e-7, 1e-6, 1e-5 and 1e-4.
+With --outdoor: the full 546k-triangle outdoor scene, every GPU form against both oracles.
 
 Test infrastructure: the oracle is the checker here, never a path of the product.
 """
@@ -63,11 +65,44 @@ def total(flips):
     return sum(v["flips"] for v in flips.values())
 
 
+def outdoor_report():
+    """The 546k-triangle outdoor scene (C4) in full: the three GPU forms against the binary32
+    oracle (the reference restatement) and the FP64 oracle, masks and bounce."""
+    import os
+    inp, opts = scenes.outdoor()
+    threads = os.cpu_count() or 1
+    t0 = time.time()
+    ref32 = oracle.bake_ex(inp, opts, mode=oracle.F32, threads=threads, bounce_maps=True)
+    t32 = time.time() - t0
+    t0 = time.time()
+    ref64 = oracle.bake_ex(inp, opts, mode=oracle.F64, threads=threads, bounce_maps=True)
+    t64 = time.time() - t0
+    out = {"report": "precision", "workload": "outdoor", "triangles": int(inp.triangle_count()),
+           "texels": int(ref32["scene"].stats["texels"]), "oracle_threads": threads,
+           "oracle_f32_s": round(t32, 1), "oracle_f64_s": round(t64, 1),
+           "oracle_f32_vs_f64_flips": compare.bit_flips(ref32["scene"], ref64["scene"]),
+           "oracle_f32_bounce_error_vs_f64": compare.bounce_error(ref32["maps"], ref64["maps"])}
+    for form in ("batched", "plain", "refined"):
+        scene, maps, rep = gpu_with_maps(inp, opts, form)
+        out[form] = {"words_equal_reference": bool(scene.words_equal(ref32["scene"])),
+                     "stats_equal_reference": scene.stats == ref32["scene"].stats,
+                     "flips_vs_reference": compare.bit_flips(scene, ref32["scene"]),
+                     "flips_vs_fp64": compare.bit_flips(scene, ref64["scene"]),
+                     "bounce_error_vs_reference": compare.bounce_error(maps, ref32["maps"]),
+                     "bounce_error_vs_fp64": compare.bounce_error(maps, ref64["maps"]),
+                     "retests": int(rep.retests), "ms_device": round(rep.ms_device, 1)}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--full-grid", type=int, default=1024)
+    ap.add_argument("--outdoor", action="store_true",
+                    help="compare the GPU forms with both oracles on the full outdoor scene instead")
     args = ap.parse_args()
+    if args.outdoor:
+        return outdoor_report()
     out = {"report": "precision", "workload": "precision_stress"}
 
     # 1. the full scene
