@@ -31,6 +31,7 @@ DIRECT, SINGLE_BOUNCE = 0, 1
 TRANSPARENCY_DISABLED, TRANSPARENCY_ENABLED, TRANSPARENCY_ENABLED_MAX = 0, 1, 2
 LIGHTING_ONLY, DISTANCE_CUBES, ANGULAR = 0, 1, 2
 FORM_BATCHED, FORM_PLAIN, FORM_REFINED = 0, 1, 2
+DEFAULT_REFINE_EPSILON = 1e-4  # dl_bake_config.refine_epsilon when left 0
 FORMS = {"batched": FORM_BATCHED, "plain": FORM_PLAIN, "refined": FORM_REFINED}
 
 ERROR_KINDS = {1: "Cancelled", 2: "DuplicateId", 3: "InvalidMesh", 4: "InvalidLight",

@@ -1537,7 +1537,7 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
         g_error = "refine_epsilon must lie in [0, 0.01]";
         return DL_INVALID_ARGUMENT;
     }
-    if (eps == 0.0f) s->config.refine_epsilon = 1.0e-5f;
+    if (eps == 0.0f) s->config.refine_epsilon = 1.0e-4f;
     std::string err;
     auto t_prep = std::chrono::steady_clock::now();
     dl_status st = prepare_scene(*in, *o, s->host, err);

@@ -254,6 +254,12 @@ __device__ bool traverse(const DevScene &sc, f3 o, f3 dir, float max, bool alpha
                                  : tri_test(v0, ldg4(sc.tri_e1 + i), ldg4(sc.tri_e2 + i), o, d, max, t, u, v);
                 if (!ok) continue;
                 uint32_t occ = __float_as_uint(v0.w);
+                // the refined form orders closest-hit candidates by their binary64 distance (and
+                // takes their barycentrics from it), so the winner is the binary64 intersection's
+                if (!ANY && REFINE) {
+                    ++vis->retests;
+                    if (!tri_test_fp64(sc, occ, o, d, max, t, u, v)) continue;
+                }
                 if (alpha && !alpha_blocks(sc, occ, u, v)) continue;
                 if (ANY) return true;
                 if (isfinite(t) && (t < hit.t || (t == hit.t && occ < hit.occluder))) {

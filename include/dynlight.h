@@ -140,11 +140,12 @@ typedef struct dl_progress {
 } dl_progress;
 
 /* How the bake runs. BATCHED and PLAIN give identical bytes, bit-exact with the reference's
-   binary32 arithmetic. REFINED is the batched form with two precision changes: ray/triangle tests
-   whose binary32 barycentrics, determinant or hit distance fall within `refine_epsilon` of a
-   boundary are re-tested in binary64, and soft-visibility weights and bounce gathers are summed
-   with compensated (Kahan) sums. Its bytes may differ from the other forms where those re-tests
-   or sums change a level. */
+   binary32 arithmetic. REFINED is the batched form with three precision changes: ray/triangle
+   tests whose binary32 barycentrics, determinant or hit distance fall within `refine_epsilon` of
+   a boundary are re-tested in binary64; closest hits are chosen by the candidates' binary64
+   distances (with their barycentrics); soft-visibility weights and bounce gathers are summed
+   with compensated (Kahan) sums. Its bytes may differ from the other forms where those change a
+   level. */
 enum {
     DL_FORM_BATCHED = 0, /* every (triangle, light) pair through one persistent kernel fed by a
                             device work queue, launched from a CUDA graph */
@@ -165,7 +166,7 @@ typedef struct dl_bake_config {
     uint32_t count_visits;     /* 1: run the instrumented visibility kernel that counts BVH node
                                   visits and triangle tests (for roofline accounting; slower) */
     float refine_epsilon;      /* DL_FORM_REFINED: re-test margin (barycentric units; times
-                                  max(1, ray length) for distances), 0: 1e-5 */
+                                  max(1, ray length) for distances), 0: 1e-4 */
     uint32_t no_autotune;      /* 1: never time candidate launch shapes; unset knobs take defaults.
                                   0: knobs left 0 are picked by timing trials on the first run of a
                                   scene shape (cached per process) */
@@ -198,7 +199,8 @@ typedef struct dl_bake_report {
                                  serialization+crop+packing, unused */
     double ms_host[4];        /* host time of session creation: validation + sorting + lights,
                                  occluder BVH build, flattening + uploads, unused */
-    uint64_t retests;         /* DL_FORM_REFINED: ray/triangle tests re-run in binary64 */
+    uint64_t retests;         /* DL_FORM_REFINED: ray/triangle tests re-run in binary64 (tests
+                                 near a boundary, and every closest-hit candidate) */
     /* launch shape of the batched visibility kernel (picked by the autotuner or the config) */
     uint32_t tuned_chunk_texels, tuned_sample_lanes, tuned_blocks_per_sm, tuned_stack_depth;
     uint32_t tuned_min_blocks;  /* launch bound: blocks per SM the registers were sized for */

@@ -99,7 +99,7 @@ def bake(inp, options, threads=0, brute_force=False, progress=None):
         lb.oracle_free(out)
 
 
-def bake_ex(inp, options, mode=F32, eps=1.0e-5, threads=0, brute_force=False, bounce_maps=False):
+def bake_ex(inp, options, mode=F32, eps=1.0e-4, threads=0, brute_force=False, bounce_maps=False):
     """Runs the oracle bake in precision `mode`. Returns a dict with the BakedScene ("scene"),
     "burial_rays", "photon_rays", "retests" and, with bounce_maps, every filtered bounce map as
     {(mesh id, slot): (window, float32 [h, w, 3])} under "maps"."""

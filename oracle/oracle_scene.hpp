@@ -688,7 +688,15 @@ struct Occluders {
         auto consider = [&](uint32_t i) {
             float t;
             V3 w;
-            if (!hit(i, o, d, max, alpha, t, w)) return;
+            if (precision().mode == PREC_REFINED) {
+                // candidates ordered by their binary64 distance, barycentrics from it too
+                if (!intersect(triangles[i].v, o, d, max, t, w)) return;
+                retest_count().fetch_add(1, std::memory_order_relaxed);
+                if (!intersect_f64(triangles[i].v, o, d, max, t, w)) return;
+                if (alpha && !blocks(triangles[i], w)) return;
+            } else if (!hit(i, o, d, max, alpha, t, w)) {
+                return;
+            }
             if (std::isfinite(t) && (!found || t < best || (t == best && i < best_i))) {
                 found = true;
                 best = t;

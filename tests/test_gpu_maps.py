@@ -53,7 +53,7 @@ def test_outdoor_maps_with_alpha_and_the_refined_form():
     got = dl.bake(inp, opts)
     assert_same(got, want)
     assert_maps(got, want)
-    refined_want = oracle.bake_ex(inp, opts, mode=oracle.REFINED, eps=1e-5)["scene"]
+    refined_want = oracle.bake_ex(inp, opts, mode=oracle.REFINED, eps=dl.DEFAULT_REFINE_EPSILON)["scene"]
     refined = dl.bake(inp, opts, form="refined")
     assert_same(refined, refined_want)
     assert refined.maps_equal(refined_want)

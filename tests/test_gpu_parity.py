@@ -221,7 +221,7 @@ def test_gather_sample_lanes_do_not_change_the_bytes(lanes):
         got = dl.bake(i, o, sample_lanes=lanes, report=report)
         assert_same(got, want)
         assert report.tuned_gather_lanes == lanes
-    refined_want = oracle.bake_ex(sun_inp, sun_opts, mode=oracle.REFINED, eps=1e-5)["scene"]
+    refined_want = oracle.bake_ex(sun_inp, sun_opts, mode=oracle.REFINED, eps=dl.DEFAULT_REFINE_EPSILON)["scene"]
     assert_same(dl.bake(sun_inp, sun_opts, form="refined", sample_lanes=lanes), refined_want)
 
 

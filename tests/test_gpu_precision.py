@@ -24,7 +24,7 @@ def _stress_slice():
 @pytest.fixture(scope="module")
 def stress():
     inp, opts = _stress_slice()
-    bakes = {name: oracle.bake_ex(inp, opts, mode=mode, eps=1e-5, bounce_maps=True)
+    bakes = {name: oracle.bake_ex(inp, opts, mode=mode, eps=dl.DEFAULT_REFINE_EPSILON, bounce_maps=True)
              for name, mode in (("f32", oracle.F32), ("refined", oracle.REFINED), ("f64", oracle.F64))}
     return inp, opts, bakes
 
@@ -64,7 +64,7 @@ def test_refined_form_matches_the_refined_oracle(stress):
     assert report.retests > 0
 
 
-@pytest.mark.parametrize("eps", [1e-7, 1e-6, 1e-4])
+@pytest.mark.parametrize("eps", [1e-7, 1e-6, 1e-5])
 def test_refined_epsilon_sweep_matches_the_oracle(eps):
     inp, opts = scenes.precision_stress(grid=40, chunks=2, boxes=8, decals=600, slivers=120, lights=10,
                                         sky_samples=16, bounce_samples=8)
@@ -76,7 +76,7 @@ def test_refined_epsilon_sweep_matches_the_oracle(eps):
 def test_refined_form_on_mixed_lights_and_alpha():
     # every light kind (src/bake/tests/determinism.rs:11-44) and an alpha-tested occluder
     inp, opts = fx.determinism_room()
-    want = oracle.bake_ex(inp, opts, mode=oracle.REFINED, eps=1e-5)["scene"]
+    want = oracle.bake_ex(inp, opts, mode=oracle.REFINED, eps=dl.DEFAULT_REFINE_EPSILON)["scene"]
     got, _, _ = _gpu(inp, opts, "refined")
     assert_same(got, want)
     plane = fx.floor(1, (0, 1.0, 0), 1.0)
@@ -85,7 +85,7 @@ def test_refined_form_on_mixed_lights_and_alpha():
     inp = dl.BakeInput([plane, fx.floor(2, (0, 0, 0), 2.0)],
                        [fx.point_light(5, (0.1, 3.0, 0.2), 6.0, transparency=dl.TRANSPARENCY_ENABLED)])
     opts = fx.options(pixel_density=16.0)
-    want = oracle.bake_ex(inp, opts, mode=oracle.REFINED, eps=1e-5)["scene"]
+    want = oracle.bake_ex(inp, opts, mode=oracle.REFINED, eps=dl.DEFAULT_REFINE_EPSILON)["scene"]
     got, _, _ = _gpu(inp, opts, "refined")
     assert_same(got, want)
 
