@@ -426,8 +426,10 @@ __global__ void __launch_bounds__(kBlock, MINB) k_trace_batched(DevScene sc, Tra
                     off.y = rng.next_f32();
                     f3 side, across;
                     ortho_pair(nrm, side, across);
-                    for (uint32_t j = sub; j < sc.sky_samples; j += W)
+                    for (uint32_t k = sub; k < sc.sky_samples; k += W) {
+                        uint32_t j = sc.sky_order ? sc.sky_order[k] : k;
                         if (!tr(cosine_direction_basis(nrm, side, across, spread(j, off, true)), INFINITY)) ++open;
+                    }
                 }
                 for (uint32_t o = 1; o < W; o <<= 1) open += __shfl_xor_sync(0xFFFFFFFFu, open, o);
                 if (valid && sub == 0) {
@@ -1665,6 +1667,9 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     sc.area_samples = o->area_light_samples;
     sc.area_min_samples = o->area_light_min_samples;
     sc.sky_samples = o->sky_samples;
+    std::vector<uint16_t> sky_order = sky_sample_order(o->sky_samples);
+    sc.sky_order = nullptr;
+    if (!sky_order.empty()) up(sky_order.data(), sky_order.size() * 2, sc.sky_order);
     sc.colored_bounce = o->colored_bounce;
     sc.refine_eps = s->config.refine_epsilon;
     sc.refine_eps2 = sc.refine_eps * sc.refine_eps;

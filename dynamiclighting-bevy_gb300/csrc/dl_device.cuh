@@ -45,6 +45,8 @@ struct DevScene {
     uint32_t colored_bounce;
     // refined form: the epsilon of the binary64 re-test and its square
     float refine_eps, refine_eps2;
+    // sky samples in a coherent order (see sky_sample_order), or null
+    const uint16_t *sky_order;
 };
 enum : uint32_t { kMeshNormals = 1, kMeshOccludes = 2, kMeshAlpha = 4 };
 

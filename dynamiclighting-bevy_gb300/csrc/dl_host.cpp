@@ -714,6 +714,27 @@ struct Writer {
 };
 }  // namespace
 
+std::vector<uint16_t> sky_sample_order(uint32_t n) {
+    if (n < 16 || n > 65536 || (n & (n - 1))) return {};
+    uint32_t m = 0;
+    while ((1u << m) < n) ++m;
+    auto spread_bits = [](uint32_t v) {  // bit i of v to bit 2i
+        uint32_t r = 0;
+        for (int i = 0; i < 16; ++i) r |= ((v >> i) & 1u) << (2 * i);
+        return r;
+    };
+    std::vector<std::pair<uint32_t, uint32_t>> keyed;
+    for (uint32_t j = 0; j < n; ++j) {
+        uint32_t cx = rev_bits(j) >> (32 - (m + 1) / 2);  // the first coordinate's top bits
+        uint32_t cy = sobol2(j) >> (32 - m / 2);           // the second's
+        keyed.push_back({spread_bits(cx) | (spread_bits(cy) << 1), j});
+    }
+    std::sort(keyed.begin(), keyed.end());
+    std::vector<uint16_t> order(n);
+    for (uint32_t r = 0; r < n; ++r) order[r] = (uint16_t)keyed[r].second;
+    return order;
+}
+
 // ---- maps for moving meshes: host halves -------------------------------------------------------
 
 // Calls f(vertex) for every corner of every occluder triangle (sun_map.rs:164-170).

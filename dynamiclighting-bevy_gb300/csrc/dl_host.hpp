@@ -82,6 +82,14 @@ dl_status prepare_scene(const dl_bake_input &in, const dl_bake_options &o, HostS
 // Builds the occluder BVH (binned SAH, leaves of at most 4 triangles, depth capped at 60).
 void build_bvh(HostScene &s);
 
+// The first n = 2^m points of the sky's low-discrepancy sequence (src/bake/spread.rs:16-24) form
+// a (0, m, 2)-net: one point in each cell of a 2^ceil(m/2) x 2^floor(m/2) grid of the unit square.
+// Listed in the Morton order of their cells, any 16 consecutive entries lie in one 4 x 4 block
+// of cells, so lanes that trace them together send nearby directions from the same texel. The
+// open count of a sky texel does not depend on the order its samples are traced in. Empty
+// unless n is a power of two from 16 to 65536.
+std::vector<uint16_t> sky_sample_order(uint32_t n);
+
 // A sun map's frame and bounds (src/bake/sun_map.rs:25-45,83-161): `empty` when there is no
 // static geometry (one texel that nothing is behind).
 struct SunMapSetup {

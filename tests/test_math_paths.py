@@ -19,3 +19,13 @@ def test_double_float_sincos_equals_the_binary64_path(tmp_path):
     for fields in lines:
         assert int(fields[-3]) == 0, out.stdout  # mismatches
         assert int(fields[-1]) < 2000000 // 1000, out.stdout  # the binary64 path is rare
+
+
+def test_sky_sample_order_is_a_clustered_permutation(tmp_path):
+    exe = tmp_path / "order_check"
+    csrc = os.path.join(ROOT, "dynamiclighting-bevy_gb300", "csrc")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-pthread", "-ffp-contract=off", "-fno-fast-math", "-x", "c++",
+                    "-I", csrc, os.path.join(ROOT, "tests", "native", "order_check.cpp"),
+                    os.path.join(csrc, "dl_host.cpp"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0 and "failures 0" in out.stdout, out.stdout
