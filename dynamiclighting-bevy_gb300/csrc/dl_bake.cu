@@ -557,14 +557,18 @@ struct BounceArgs {
     uint32_t lanes;         // lanes sharing one texel's samples (1, 2, 4, 8, 16 or 32)
     uint32_t sample_every;  // tuning trials: one claimed step in `sample_every` (1: all)
     uint32_t stack_depth;   // shared-memory stack entries per thread
+    uint32_t buffered;      // samples each lane group can buffer for the coherent order (0: none)
     unsigned long long *head;  // steps claimed so far (32 / lanes items per step)
 };
 
 // gather_triangle / gather_sun (bounce.rs:235-292, sun_bounce.rs:24-80): a group of `lanes`
 // lanes per (bounce pair, texel) item. Each round, lane k of a group evaluates sample
 // round * lanes + k; the group leader then adds the round's contributions in sample order, so
-// the sum is the reference's sequential one for any group size. Dynamic shared memory holds the
-// traversal stacks and one float4 contribution slot per thread. MINB is the launch bound's
+// the sum is the reference's sequential one for any group size. Sun gathers with a power-of-two
+// sample count up to `buffered` instead take their samples in the coherent order of the sample
+// net (sample_order: a group's lanes send nearby directions together), buffer every sample's
+// contribution and let the leader add them in sample order at the end. Dynamic shared memory
+// holds the traversal stacks, one float4 contribution slot per thread and the groups' buffers. MINB is the launch bound's
 // blocks per SM (the register budget: 6 leaves the compiler its 80 registers, 8 asks for 64).
 template <bool REFINE, int MINB>
 __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs a) {
@@ -572,6 +576,8 @@ __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs
     int *my = smem + threadIdx.x;
     float4 *part = reinterpret_cast<float4 *>(smem + (size_t)a.stack_depth * kBlock);
     const uint32_t lane = lane_id(), W = a.lanes, sub = lane % W, per_step = 32 / W;
+    // this lane group's buffer of `buffered` contributions
+    float4 *buf = part + kBlock + (size_t)((threadIdx.x >> 5) * per_step + lane / W) * a.buffered;
     unsigned long long rays = 0;
     Visits vis{0, 0, 0};
     for (;;) {
@@ -614,10 +620,12 @@ __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs
             }
         }
         if (!active) samples = 0;
+        const uint16_t *order = sun && samples <= a.buffered ? sample_order(sc, samples) : nullptr;
         FSum3<REFINE> sum;
         const uint32_t rounds = __reduce_max_sync(0xFFFFFFFFu, (samples + W - 1) / W);
         for (uint32_t r = 0; r < rounds; ++r) {
-            uint32_t i = r * W + sub;
+            uint32_t k = r * W + sub;
+            uint32_t i = order && k < samples ? order[k] : k;
             Contribution c{f3{0.0f, 0.0f, 0.0f}, false, 0};
             if (i < samples) {
                 const DevLight &l = sc.lights[s];
@@ -630,16 +638,28 @@ __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs
                 }
                 rays += c.rays;
             }
-            part[threadIdx.x] = make_float4(c.value.x, c.value.y, c.value.z, c.add ? 1.0f : 0.0f);
+            float4 cv = make_float4(c.value.x, c.value.y, c.value.z, c.add ? 1.0f : 0.0f);
+            if (order) {
+                if (i < samples) buf[i] = cv;
+            } else {
+                part[threadIdx.x] = cv;
+            }
             __syncwarp();
-            if (sub == 0 && samples) {
-                for (uint32_t k = 0; k < W && r * W + k < samples; ++k) {
-                    float4 q = part[threadIdx.x + k];
+            if (!order && sub == 0 && samples) {
+                for (uint32_t j = 0; j < W && r * W + j < samples; ++j) {
+                    float4 q = part[threadIdx.x + j];
                     if (q.w != 0.0f) sum.add(f3{q.x, q.y, q.z});
                 }
             }
             __syncwarp();
         }
+        if (order && sub == 0) {
+            for (uint32_t j = 0; j < samples; ++j) {
+                float4 q = buf[j];
+                if (q.w != 0.0f) sum.add(f3{q.x, q.y, q.z});
+            }
+        }
+        __syncwarp();
         if (valid && sub == 0) {
             f3 v{0.0f, 0.0f, 0.0f};
             if (active) v = divs(scale(sum.value(), sc.lights[s].bounce_intensity), (float)samples);
@@ -1667,9 +1687,19 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     sc.area_samples = o->area_light_samples;
     sc.area_min_samples = o->area_light_min_samples;
     sc.sky_samples = o->sky_samples;
+    std::vector<uint16_t> orders;
+    for (uint32_t n = 16; n <= kMaxOrdered; n *= 2) {
+        std::vector<uint16_t> o16 = sky_sample_order(n);
+        orders.insert(orders.end(), o16.begin(), o16.end());
+    }
     std::vector<uint16_t> sky_order = sky_sample_order(o->sky_samples);
+    up(orders.data(), orders.size() * 2, sc.orders);
     sc.sky_order = nullptr;
-    if (!sky_order.empty()) up(sky_order.data(), sky_order.size() * 2, sc.sky_order);
+    if (o->sky_samples <= kMaxOrdered && !sky_order.empty()) {
+        sc.sky_order = sc.orders + (o->sky_samples - 16);
+    } else if (!sky_order.empty()) {
+        up(sky_order.data(), sky_order.size() * 2, sc.sky_order);
+    }
     sc.colored_bounce = o->colored_bounce;
     sc.refine_eps = s->config.refine_epsilon;
     sc.refine_eps2 = sc.refine_eps * sc.refine_eps;
@@ -1803,7 +1833,7 @@ TraceTune trace_tune(dl_session &s, TraceArgs ta, bool refine, bool count, dl_pr
 // The gather kernel's lanes per texel, tuned the same way (trials on every k-th step of the real
 // item list, value writes that the real pass overwrites).
 struct GatherTune {
-    uint32_t lanes = 1, minb = 6, stack_depth = kStack, blocks = 1, trials = 0;
+    uint32_t lanes = 1, minb = 6, stack_depth = kStack, blocks = 1, trials = 0, buffered = 0;
     double ms = 0.0;
 };
 using GatherKernel = void (*)(DevScene, BounceArgs);
@@ -1811,27 +1841,45 @@ GatherKernel gather_kernel(bool refine, uint32_t minb) {
     if (refine) return k_gather<true, 6>;
     return minb == 8 ? k_gather<false, 8> : k_gather<false, 6>;
 }
-size_t gather_smem(uint32_t depth) { return (size_t)depth * kBlock * sizeof(int) + kBlock * sizeof(float4); }
+// Shared memory of a gather launch: stacks, the round slots and, for the coherent order, a
+// buffer of `buffered` contributions per lane group.
+size_t gather_smem(uint32_t depth, uint32_t lanes, uint32_t buffered) {
+    return (size_t)depth * kBlock * sizeof(int) + kBlock * sizeof(float4) +
+           (size_t)(kBlock / lanes) * buffered * sizeof(float4);
+}
+// The buffer for coherent sun gathers: the largest power-of-two sun bounce sample count up to
+// 256, for groups of 16 or 32 lanes (0 otherwise).
+uint32_t gather_buffer(const HostScene &h, uint32_t lanes) {
+    if (lanes < 16) return 0;
+    uint32_t most = 0;
+    for (const DevLight &l : h.lights)
+        if (l.shape == DL_SHAPE_SUN && (l.flags & kLightBounce)) {
+            uint32_t n = l.bounce_samples;
+            if (n >= 16 && n <= 256 && !(n & (n - 1))) most = std::max(most, n);
+        }
+    return most;
+}
 std::map<TuneKey, GatherTune> g_gather_cache;
 
 GatherTune gather_tune(dl_session &s, BounceArgs ba, uint32_t bpairs, bool refine, dl_progress *progress) {
     const dl_bake_config &c = s.config;
     GatherTune best;
     best.stack_depth = std::max<uint32_t>(8, (s.host.bvh_depth + 3) & ~3u);
-    auto blocks_for = [&](uint32_t minb) {
+    auto blocks_for = [&](uint32_t minb, uint32_t w) {
         int per_sm = 0;
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gather_kernel(refine, minb), kBlock,
-                                                         gather_smem(best.stack_depth)));
+                                                         gather_smem(best.stack_depth, w, gather_buffer(s.host, w))));
         if (c.blocks_per_sm) per_sm = std::min(per_sm, (int)c.blocks_per_sm);
         return (uint32_t)std::max(1, per_sm) * (uint32_t)s.sms;
     };
     std::vector<uint32_t> lanes = c.sample_lanes ? std::vector<uint32_t>{c.sample_lanes}
-                                                 : std::vector<uint32_t>{1, 4, 8, 16};
+                                                 : std::vector<uint32_t>{1, 4, 8, 16, 32};
     std::vector<uint32_t> minbs = refine ? std::vector<uint32_t>{6} : std::vector<uint32_t>{6, 8};
     const uint32_t every = ba.items >= (1u << 20) ? 8 : ba.items >= (1u << 18) ? 4 : 0;
     best.lanes = lanes[0];
     best.minb = minbs[0];
-    best.blocks = blocks_for(best.minb);
+    best.buffered = gather_buffer(s.host, best.lanes);
+    best.blocks = blocks_for(best.minb, best.lanes);
     if (c.no_autotune || !every || lanes.size() * minbs.size() == 1 || (progress && progress->cancel))
         return best;
     TuneKey key{s.device, ba.items, bpairs, 0, s.host.tri_v0.size(), s.host.nodes.size(), best.stack_depth,
@@ -1856,12 +1904,14 @@ GatherTune gather_tune(dl_session &s, BounceArgs ba, uint32_t bpairs, bool refin
     float best_ms = INFINITY;
     auto t0 = std::chrono::steady_clock::now();
     for (uint32_t minb : minbs) {
-        uint32_t blocks = blocks_for(minb);
         for (uint32_t w : lanes) {
+            uint32_t blocks = blocks_for(minb, w);
             ba.lanes = w;
+            ba.buffered = gather_buffer(s.host, w);
             CK(cudaMemsetAsync(ba.head, 0, sizeof(unsigned long long), st));
             CK(cudaEventRecord(a, st));
-            gather_kernel(refine, minb)<<<blocks, kBlock, gather_smem(best.stack_depth), st>>>(s.sc, ba);
+            gather_kernel(refine, minb)<<<blocks, kBlock, gather_smem(best.stack_depth, w, ba.buffered), st>>>(
+                s.sc, ba);
             CK(cudaGetLastError());
             CK(cudaEventRecord(b, st));
             CK(cudaEventSynchronize(b));
@@ -1873,6 +1923,7 @@ GatherTune gather_tune(dl_session &s, BounceArgs ba, uint32_t bpairs, bool refin
                 best.lanes = w;
                 best.minb = minb;
                 best.blocks = blocks;
+                best.buffered = ba.buffered;
             }
         }
     }
@@ -2289,11 +2340,13 @@ dl_status run(dl_session &s, dl_progress *progress) {
             GatherTune g = gather_tune(s, ba, bcount, refine, progress);
             ba.lanes = g.lanes;
             ba.stack_depth = g.stack_depth;
+            ba.buffered = g.buffered;
             s.report.tuned_gather_lanes = g.lanes;
             s.report.tune_trials += g.trials;
             s.report.ms_tune += g.ms;
             CK(cudaMemsetAsync(ba.head, 0, sizeof(unsigned long long), st));
-            gather_kernel(refine, g.minb)<<<g.blocks, kBlock, gather_smem(g.stack_depth), st>>>(sc, ba);
+            gather_kernel(refine, g.minb)<<<g.blocks, kBlock, gather_smem(g.stack_depth, g.lanes, g.buffered), st>>>(
+                sc, ba);
             LAUNCHED("k_gather");
             ++s.launches;
         }

@@ -45,9 +45,16 @@ struct DevScene {
     uint32_t colored_bounce;
     // refined form: the epsilon of the binary64 re-test and its square
     float refine_eps, refine_eps2;
-    // sky samples in a coherent order (see sky_sample_order), or null
+    // coherent sample orders (sky_sample_order) for n = 16, 32, ..., kMaxOrdered back to back
+    // (the table of n starts at n - 16); sky_order is the sky's, or null
+    const uint16_t *orders;
     const uint16_t *sky_order;
 };
+constexpr uint32_t kMaxOrdered = 4096;
+// The coherent order of n samples, or null when n is not a power of two from 16 to kMaxOrdered.
+__device__ __forceinline__ const uint16_t *sample_order(const DevScene &sc, uint32_t n) {
+    return (n >= 16 && n <= kMaxOrdered && !(n & (n - 1))) ? sc.orders + (n - 16) : nullptr;
+}
 enum : uint32_t { kMeshNormals = 1, kMeshOccludes = 2, kMeshAlpha = 4 };
 
 __device__ __forceinline__ float4 ldg4(const float4 *p) { return __ldg(p); }

@@ -210,19 +210,25 @@ def test_sky_sample_lanes_do_not_change_the_bytes(lanes):
 
 @pytest.mark.parametrize("lanes", [1, 4, 16, 32])
 def test_gather_sample_lanes_do_not_change_the_bytes(lanes):
-    # lanes sharing one texel's bounce samples add them in sample order: the reference's sums
+    # lanes sharing one texel's bounce samples add them in sample order: the reference's sums;
+    # sun bounces of 16 to 256 samples (a power of two) are traced in the coherent net order by
+    # groups of 16 or 32 lanes and still summed in sample order
     inp, opts = scenes.room_grid(rooms=1, lights=4, boxes_per_room=3, samples=24)
     opts.photon_cube_resolution = 48
     sun_inp, sun_opts = scenes.outdoor(grid=33, chunks=2, boxes=12, point_lights=2, sky_samples=16,
                                        bounce_samples=24)
-    for case, (i, o) in enumerate(((inp, opts), (sun_inp, sun_opts))):
+    cases = [(inp, opts), (sun_inp, sun_opts)]
+    cases += [scenes.outdoor(grid=33, chunks=2, boxes=12, point_lights=2, sky_samples=16, bounce_samples=n)
+              for n in (16, 64, 256)]
+    for case, (i, o) in enumerate(cases):
         want, _, _ = oracle.bake(i, o)
         report = dl._abi.DlBakeReport()
         got = dl.bake(i, o, sample_lanes=lanes, report=report)
         assert_same(got, want)
         assert report.tuned_gather_lanes == lanes
-    refined_want = oracle.bake_ex(sun_inp, sun_opts, mode=oracle.REFINED, eps=dl.DEFAULT_REFINE_EPSILON)["scene"]
-    assert_same(dl.bake(sun_inp, sun_opts, form="refined", sample_lanes=lanes), refined_want)
+    for i, o in (cases[1], cases[3]):
+        refined_want = oracle.bake_ex(i, o, mode=oracle.REFINED, eps=dl.DEFAULT_REFINE_EPSILON)["scene"]
+        assert_same(dl.bake(i, o, form="refined", sample_lanes=lanes), refined_want)
 
 
 def test_autotuned_launch_shape_gives_the_default_bytes():
