@@ -2490,42 +2490,56 @@ dl_status run(dl_session &s, dl_progress *progress) {
     return DL_OK;
 }
 
-// Host buffers of freed results' words, handed to the next result so that its download writes
-// pages that are already mapped (a fresh buffer of this size spends most of its copy time in
-// first-touch page faults). At most kCacheBytes are held.
+// Host buffers of freed results' words, handed to the next result. They are pinned (page-locked)
+// when the driver allows it, so that the download runs as a DMA copy at the link's rate instead
+// of through the driver's staging buffers, and a reused buffer needs no first-touch page faults
+// either. At most kCacheBytes are held.
 struct WordCache {
     static constexpr size_t kCacheBytes = size_t(2) << 30;
+    struct Buffer {
+        size_t cap;  // words
+        uint32_t *p;
+        bool pinned;
+    };
     std::mutex lock;
-    std::vector<std::pair<size_t, uint32_t *>> free;  // (capacity in words, buffer)
+    std::vector<Buffer> free;
     size_t held = 0;
-    uint32_t *take(size_t n, size_t &cap) {
-        std::lock_guard<std::mutex> guard(lock);
-        size_t best = free.size();
-        for (size_t i = 0; i < free.size(); ++i)
-            if (free[i].first >= n && (best == free.size() || free[i].first < free[best].first)) best = i;
-        if (best < free.size()) {
-            auto e = free[best];
-            free.erase(free.begin() + best);
-            held -= e.first * 4;
-            cap = e.first;
-            return e.second;
-        }
-        cap = n;
-        return new uint32_t[n ? n : 1];
+    static void release(const Buffer &b) {
+        if (b.pinned) cudaFreeHost(b.p);  // fails harmlessly once the runtime has shut down at exit
+        else delete[] b.p;
     }
-    void give(uint32_t *p, size_t cap) {
+    Buffer take(size_t n) {
+        {
+            std::lock_guard<std::mutex> guard(lock);
+            size_t best = free.size();
+            for (size_t i = 0; i < free.size(); ++i)
+                if (free[i].cap >= n && (best == free.size() || free[i].cap < free[best].cap)) best = i;
+            if (best < free.size()) {
+                Buffer b = free[best];
+                free.erase(free.begin() + best);
+                held -= b.cap * 4;
+                return b;
+            }
+        }
+        size_t cap = n ? n : 1;
+        void *p = nullptr;
+        if (cudaHostAlloc(&p, cap * 4, cudaHostAllocPortable) == cudaSuccess) return Buffer{cap, (uint32_t *)p, true};
+        cudaGetLastError();  // no pinned memory to be had: a pageable buffer (a slower copy)
+        return Buffer{cap, new uint32_t[cap], false};
+    }
+    void give(const Buffer &b) {
         std::lock_guard<std::mutex> guard(lock);
-        while (held + cap * 4 > kCacheBytes && !free.empty()) {  // drop the oldest
-            held -= free.front().first * 4;
-            delete[] free.front().second;
+        while (held + b.cap * 4 > kCacheBytes && !free.empty()) {  // drop the oldest
+            held -= free.front().cap * 4;
+            release(free.front());
             free.erase(free.begin());
         }
-        if (cap * 4 > kCacheBytes) {
-            delete[] p;
+        if (b.cap * 4 > kCacheBytes) {
+            release(b);
             return;
         }
-        free.emplace_back(cap, p);
-        held += cap * 4;
+        free.push_back(b);
+        held += b.cap * 4;
     }
 };
 WordCache &word_cache() {
@@ -2539,10 +2553,10 @@ struct HostResult {
     std::vector<dl_baked_light> lights;
     std::vector<dl_light_bvh_node> bvh;
     std::vector<dl_baked_mesh> meshes;
-    uint32_t *words = nullptr;  // from word_cache(), `words_cap` words
-    size_t words_cap = 0;
+    uint32_t *words = nullptr;  // buffer.p
+    WordCache::Buffer buffer{0, nullptr, false};  // from word_cache()
     ~HostResult() {
-        if (words) word_cache().give(words, words_cap);
+        if (buffer.p) word_cache().give(buffer);
     }
     std::vector<uint32_t> cubes;
     std::vector<std::vector<uint32_t>> sun_words;
@@ -2563,7 +2577,8 @@ dl_status assemble(dl_session &s, std::unique_ptr<HostResult> &r, bool download)
     const HostScene &h = s.host;
     const uint32_t *words = s.words_dev;
     if (download) {
-        r->words = word_cache().take(s.out_words, r->words_cap);
+        r->buffer = word_cache().take(s.out_words);
+        r->words = r->buffer.p;
         if (s.out_words) CK(cudaMemcpy(r->words, s.words_dev, s.out_words * 4, cudaMemcpyDeviceToHost));
         words = r->words;
         s.report.d2h_bytes = s.out_words * 4 + (s.mesh_words.size() * 8) + sizeof(Counters);
