@@ -414,6 +414,9 @@ def load_library(path: str = LIBRARY_PATH):
     lib.dl_free.argtypes = [C.c_void_p]
     lib.dl_session_encode_payload.restype = C.c_int
     lib.dl_session_encode_payload.argtypes = [C.c_void_p, P(P(C.c_uint8)), P(C.c_uint64), P(C.c_uint32)]
+    lib.dl_session_occluder_bvh.restype = C.c_int
+    lib.dl_session_occluder_bvh.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64,
+                                            P(C.c_uint32), P(C.c_uint32)]
     lib.dl_session_bounce_map.restype = C.c_int
     lib.dl_session_bounce_map.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_void_p, C.c_void_p,
                                           C.c_uint32, P(C.c_uint32)]
@@ -524,6 +527,23 @@ class Session:
             _raise(self.lib, status)
         w, h = int(rect[2] - rect[0] + 1), int(rect[3] - rect[1] + 1)
         return tuple(int(x) for x in rect), rgb.reshape(h, w, 3)
+
+    def occluder_bvh(self):
+        """The session's occluder BVH as the traversal reads it: (nodes uint32 [n, 16] — child
+        boxes as float bits, then the two child references as int32 bits and two zero words —,
+        triangles float32 [occluders, 12] in leaf order, depth)."""
+        n, depth = C.c_uint32(), C.c_uint32()
+        status = self.lib.dl_session_occluder_bvh(self.handle, None, 0, None, 0, C.byref(n), C.byref(depth))
+        if status != 0:
+            _raise(self.lib, status)
+        occluders = int(self.report().occluders)
+        nodes = np.zeros((n.value, 16), np.uint32)
+        tris = np.zeros((occluders, 12), np.float32)
+        status = self.lib.dl_session_occluder_bvh(self.handle, nodes.ctypes.data, n.value, tris.ctypes.data,
+                                                  occluders, C.byref(n), C.byref(depth))
+        if status != 0:
+            _raise(self.lib, status)
+        return nodes, tris, depth.value
 
     def close(self):
         if self.handle:

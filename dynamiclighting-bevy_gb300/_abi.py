@@ -55,8 +55,8 @@ class DlBakeConfig(C.Structure):
     _fields_ = [("form", C.c_uint32), ("device", C.c_uint32), ("block_threads", C.c_uint32),
                 ("chunk_texels", C.c_uint32), ("sample_lanes", C.c_uint32),
                 ("blocks_per_sm", C.c_uint32), ("count_visits", C.c_uint32),
-                ("refine_epsilon", C.c_float), ("no_autotune", C.c_uint32),
-                ("reserved", C.c_uint32 * 5)]
+                ("refine_epsilon", C.c_float), ("no_autotune", C.c_uint32), ("host_bvh", C.c_uint32),
+                ("reserved", C.c_uint32 * 4)]
 
 
 class DlBakeReport(C.Structure):
@@ -140,6 +140,7 @@ EXPORTS = [
     "dl_baked_scene_free", "dl_default_options", "dl_session_create", "dl_session_run",
     "dl_session_result", "dl_session_report", "dl_session_destroy", "dl_encode_payload",
     "dl_free", "dl_filter_bounce_window_noalloc", "dl_session_bounce_map", "dl_session_encode_payload",
+    "dl_session_occluder_bvh",
 ]
 
 STATUS = {0: "ok", 1: "cancelled", 2: "duplicate id", 3: "invalid mesh", 4: "invalid light",

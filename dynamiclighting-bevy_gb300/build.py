@@ -1,7 +1,7 @@
 """Builds the CUDA library (`_build/libdynlight_gb300.so`) for sm_103a with nvcc.
 
 Device code is compiled with --fmad=false and host code with -ffp-contract=off: the bake's f32
-arithmetic must round exactly like the reference's (which never fuses a*b+c). The two
+arithmetic must round exactly like the reference's (which never fuses a*b+c). The three
 translation units compile in parallel; a full build takes about a minute.
 """
 import os
@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libdynlight_gb300.so")
-SOURCES = ["dl_bake.cu", "dl_host.cpp"]
+SOURCES = ["dl_bake.cu", "dl_bvh.cu", "dl_host.cpp"]
 
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

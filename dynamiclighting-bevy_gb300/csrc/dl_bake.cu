@@ -29,6 +29,7 @@
 #include <tuple>
 #include <vector>
 
+#include "dl_bvh.hpp"
 #include "dl_kernels.cuh"
 
 namespace dl {
@@ -1574,15 +1575,20 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
             return DL_UNSUPPORTED;
         }
     s->report.ms_host[0] = ms_since(t_prep);
-    auto t_bvh = std::chrono::steady_clock::now();
-    build_bvh(h);
-    s->report.ms_host[1] = ms_since(t_bvh);
-    auto t_up = std::chrono::steady_clock::now();
-    // the traversal stack holds one entry per level below the root
-    if (h.bvh_depth >= (uint32_t)kStack) {
-        g_error = "occluder BVH deeper than the traversal stack";
-        return DL_UNSUPPORTED;
+    // the occluder BVH: on the host's cores when asked, else on the device once the triangles
+    // are uploaded (the same tree)
+    const bool host_bvh = s->config.host_bvh != 0;
+    if (host_bvh) {
+        auto t_bvh = std::chrono::steady_clock::now();
+        build_bvh(h);
+        s->report.ms_host[1] = ms_since(t_bvh);
+        // the traversal stack holds one entry per level below the root
+        if (h.bvh_depth >= (uint32_t)kStack) {
+            g_error = "occluder BVH deeper than the traversal stack";
+            return DL_UNSUPPORTED;
+        }
     }
+    auto t_up = std::chrono::steady_clock::now();
     s->device = (int)s->config.device;
     CK(cudaSetDevice(s->device));
     CK(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device));
@@ -1639,12 +1645,6 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     s->grid_off[M] = s->grid_words;
     s->mesh_tri_base = tbase;
     uint32_t N = (uint32_t)h.occ_mesh.size();
-    std::vector<uint32_t> occ_leaf(N);
-    for (uint32_t k = 0; k < N; ++k) {
-        uint32_t occ;
-        std::memcpy(&occ, &h.tri_v0[k * 4 + 3], 4);
-        occ_leaf[occ] = k;
-    }
 
     uint64_t &bytes = s->scene_bytes;
     auto up = [&](const void *src, size_t n, auto *&dst) {
@@ -1655,14 +1655,9 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
         s->report.h2d_bytes += n;
     };
     DevScene &sc = s->sc;
-    up(h.nodes.data(), h.nodes.size() * sizeof(BvhNode), sc.nodes);
-    up(h.tri_v0.data(), h.tri_v0.size() * 4, sc.tri_v0);
-    up(h.tri_e1.data(), h.tri_e1.size() * 4, sc.tri_e1);
-    up(h.tri_e2.data(), h.tri_e2.size() * 4, sc.tri_e2);
     sc.occluders = N;
     up(h.occ_mesh.data(), N * 4ull, sc.occ_mesh);
     up(h.occ_tri.data(), N * 4ull, sc.occ_tri);
-    up(occ_leaf.data(), N * 4ull, sc.occ_leaf);
     sc.mesh_count = M;
     up(vbase.data(), vbase.size() * 4, sc.mesh_vertex_base);
     up(ibase.data(), ibase.size() * 4, sc.mesh_index_base);
@@ -1678,6 +1673,52 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     up(uv1.data(), uv1.size() * 4, sc.uv1);
     up(uv0.data(), uv0.size() * 4, sc.uv0);
     up(idx.data(), idx.size() * 4, sc.indices);
+    double ms_bvh_device = 0.0;
+    if (host_bvh) {
+        std::vector<uint32_t> occ_leaf(N);
+        for (uint32_t k = 0; k < N; ++k) {
+            uint32_t occ;
+            std::memcpy(&occ, &h.tri_v0[k * 4 + 3], 4);
+            occ_leaf[occ] = k;
+        }
+        up(h.nodes.data(), h.nodes.size() * sizeof(BvhNode), sc.nodes);
+        up(h.tri_v0.data(), h.tri_v0.size() * 4, sc.tri_v0);
+        up(h.tri_e1.data(), h.tri_e1.size() * 4, sc.tri_e1);
+        up(h.tri_e2.data(), h.tri_e2.size() * 4, sc.tri_e2);
+        up(occ_leaf.data(), N * 4ull, sc.occ_leaf);
+    } else {
+        auto t_bvh = std::chrono::steady_clock::now();
+        DeviceBvhInput bi{sc.positions, sc.indices, sc.mesh_vertex_base, sc.mesh_index_base, sc.occ_mesh,
+                          sc.occ_tri, N};
+        DeviceBvh db;
+        try {
+            build_bvh_device(bi, [&](size_t b) { return (void *)dev_alloc<uint8_t>(s->owned, b, bytes); }, s->stream,
+                             db);
+        } catch (const DeviceBvhError &e) {
+            throw CudaError{e.code, e.what};
+        }
+        ms_bvh_device = ms_since(t_bvh);
+        s->report.ms_host[1] = ms_bvh_device;
+        // the traversal stack holds one entry per level below the root
+        if (db.too_deep || db.depth >= (uint32_t)kStack) {
+            g_error = "occluder BVH deeper than the traversal stack";
+            return DL_UNSUPPORTED;
+        }
+        h.bvh_depth = db.depth;
+        h.bvh_node_count = db.node_count;
+        sc.nodes = reinterpret_cast<const float4 *>(db.nodes);
+        sc.tri_v0 = db.tri_v0;
+        sc.tri_e1 = db.tri_e1;
+        sc.tri_e2 = db.tri_e2;
+        sc.occ_leaf = db.occ_leaf;
+        if (N == 0) {  // no occluders: small placeholders, which traversal never reads
+            sc.nodes = dev_alloc<float4>(s->owned, 4, bytes);
+            sc.tri_v0 = dev_alloc<float4>(s->owned, 1, bytes);
+            sc.tri_e1 = dev_alloc<float4>(s->owned, 1, bytes);
+            sc.tri_e2 = dev_alloc<float4>(s->owned, 1, bytes);
+            sc.occ_leaf = dev_alloc<uint32_t>(s->owned, 1, bytes);
+        }
+    }
     sc.triangles = T;
     up(tri_mesh.data(), T * 4ull, sc.tri_mesh);
     sc.light_count = (uint32_t)h.lights.size();
@@ -1706,8 +1747,8 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     s->ctr = dev_alloc<Counters>(s->owned, 1, bytes);
     s->cancel_dev = dev_alloc<uint32_t>(s->owned, 1, bytes);
     for (auto &e : s->marks) CK(cudaEventCreate(&e));
-    s->report.ms_host[2] = ms_since(t_up);
-    s->report.bvh_nodes = h.nodes.size();
+    s->report.ms_host[2] = ms_since(t_up) - ms_bvh_device;
+    s->report.bvh_nodes = h.bvh_node_count;
     s->report.occluders = N;
     out = s.release();
     return DL_OK;
@@ -1775,7 +1816,7 @@ TraceTune trace_tune(dl_session &s, TraceArgs ta, bool refine, bool count, dl_pr
         best.blocks = blocks_for(best.minb);
         return best;
     }
-    TuneKey key{s.device, ta.items, ta.sky_items, ta.pairs, s.host.tri_v0.size(), s.host.nodes.size(),
+    TuneKey key{s.device, ta.items, ta.sky_items, ta.pairs, s.host.occ_mesh.size(), s.host.bvh_node_count,
                 best.stack_depth, (count ? 1u : 0u) | (refine ? 2u : 0u),
                 c.chunk_texels | (c.sample_lanes << 16) | (c.blocks_per_sm << 24)};
     {
@@ -1882,7 +1923,7 @@ GatherTune gather_tune(dl_session &s, BounceArgs ba, uint32_t bpairs, bool refin
     best.blocks = blocks_for(best.minb, best.lanes);
     if (c.no_autotune || !every || lanes.size() * minbs.size() == 1 || (progress && progress->cancel))
         return best;
-    TuneKey key{s.device, ba.items, bpairs, 0, s.host.tri_v0.size(), s.host.nodes.size(), best.stack_depth,
+    TuneKey key{s.device, ba.items, bpairs, 0, s.host.occ_mesh.size(), s.host.bvh_node_count, best.stack_depth,
                 refine ? 2u : 0u, c.blocks_per_sm};
     {
         std::lock_guard<std::mutex> guard(g_tune_lock);
@@ -2959,6 +3000,30 @@ dl_status dl_session_bounce_map(dl_session *s, uint64_t mesh_id, uint32_t slot, 
                 rgb[k * 3 + 1] = v[k].y;
                 rgb[k * 3 + 2] = v[k].z;
             }
+        }
+        return DL_OK;
+    })
+}
+
+dl_status dl_session_occluder_bvh(dl_session *s, void *nodes, uint64_t node_cap, float *triangles,
+                                  uint64_t tri_cap, uint32_t *node_count, uint32_t *depth) {
+    if (!s || !node_count || !depth || (node_cap && !nodes) || (tri_cap && !triangles)) {
+        g_error = "null argument";
+        return DL_INVALID_ARGUMENT;
+    }
+    const HostScene &h = s->host;
+    *node_count = h.bvh_node_count;
+    *depth = h.bvh_depth;
+    DL_GUARD({
+        CK(cudaSetDevice(s->device));
+        uint64_t n = std::min<uint64_t>(node_cap, h.bvh_node_count);
+        if (n) CK(cudaMemcpy(nodes, s->sc.nodes, n * sizeof(BvhNode), cudaMemcpyDeviceToHost));
+        uint64_t t = std::min<uint64_t>(tri_cap, s->sc.occluders);
+        std::vector<float4> part(t);
+        for (int j = 0; j < 3 && t; ++j) {
+            const float4 *src = j == 0 ? s->sc.tri_v0 : j == 1 ? s->sc.tri_e1 : s->sc.tri_e2;
+            CK(cudaMemcpy(part.data(), src, t * sizeof(float4), cudaMemcpyDeviceToHost));
+            for (uint64_t k = 0; k < t; ++k) std::memcpy(triangles + k * 12 + j * 4, &part[k], sizeof(float4));
         }
         return DL_OK;
     })

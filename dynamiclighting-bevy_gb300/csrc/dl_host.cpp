@@ -1,6 +1,7 @@
 // Host half of the bake (see dl_host.hpp). Compiled with -ffp-contract=off: the f32 formulas
 // here (surface areas, light bounds, light frames) must round like the reference's Rust.
 #include "dl_host.hpp"
+#include "dl_bvh_rules.hpp"
 
 #include <algorithm>
 #include <memory>
@@ -340,13 +341,6 @@ struct Ref {
     uint32_t count;
     float lo[3], hi[3];
 };
-// Build parameters; a sweep (16 or 32 bins, leaves of 2 to 7, node costs 0.3 to 2) left the
-// outdoor bake within 1 % of these, larger leaves slower.
-constexpr int kBins = 16;
-constexpr uint32_t kMaxLeaf = 4;     // at most 7 (the leaf reference's count field)
-constexpr float kNodeCost = 0.3f;    // SAH cost of a node visit, triangle tests costing 1
-constexpr uint32_t kMaxDepth = 60;
-
 // Subtrees larger than this, near the root, are built on their own threads.
 constexpr uint32_t kParallelPrims = 16384;
 constexpr uint32_t kParallelDepth = 6;
@@ -374,12 +368,6 @@ struct Builder {
     std::vector<Prim> prims;
     std::vector<uint32_t> idx;
 
-    static float half_area(const float lo[3], const float hi[3]) {
-        float e0 = hi[0] - lo[0], e1 = hi[1] - lo[1], e2 = hi[2] - lo[2];
-        if (e0 < 0 || e1 < 0 || e2 < 0) return 0.0f;
-        return e0 * e1 + e1 * e2 + e2 * e0;
-    }
-
     // Leaves are referenced as ~(first << 3 | count), count <= 7.
     Ref leaf(uint32_t first, uint32_t count, const float lo[3], const float hi[3]) {
         Ref r{~(int32_t)((first << 3) | count), count, {lo[0], lo[1], lo[2]}, {hi[0], hi[1], hi[2]}};
@@ -401,20 +389,18 @@ struct Builder {
             }
         }
     }
-    // Per-axis bins (boxes and counts) of idx[b, e) for centroid bounds clo .. clo + kBins / k.
-    struct Bins {
-        float bl[3][kBins][3], bh[3][kBins][3];
-        uint32_t bc[3][kBins];
+    // Per-axis bins (boxes and counts) of idx[b, e) for centroid bounds clo .. clo + kBvhBins / k.
+    struct Bins : BvhBins {
         void reset() {
             for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < kBins; ++b) {
+                for (int b = 0; b < kBvhBins; ++b) {
                     bc[a][b] = 0;
                     for (int j = 0; j < 3; ++j) { bl[a][b][j] = INFINITY; bh[a][b][j] = -INFINITY; }
                 }
         }
         void merge(const Bins &o) {
             for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < kBins; ++b) {
+                for (int b = 0; b < kBvhBins; ++b) {
                     bc[a][b] += o.bc[a][b];
                     for (int j = 0; j < 3; ++j) {
                         bl[a][b][j] = std::min(bl[a][b][j], o.bl[a][b][j]);
@@ -428,7 +414,7 @@ struct Builder {
             const Prim &p = prims[idx[i]];
             for (int a = 0; a < 3; ++a) {
                 if (!use[a]) continue;
-                int bb = std::min(kBins - 1, (int)((p.c[a] - clo[a]) * k[a]));
+                int bb = bvh_bin(p.c[a], clo[a], k[a]);
                 ++out.bc[a][bb];
                 for (int j = 0; j < 3; ++j) {
                     out.bl[a][bb][j] = std::min(out.bl[a][bb][j], p.lo[j]);
@@ -465,14 +451,14 @@ struct Builder {
         } else {
             bounds(first, first + count, lo, hi, clo, chi);
         }
-        if (count <= 2 || (depth >= kMaxDepth && count <= 7)) return leaf(first, count, lo, hi);
-        // SAH over kBins bins per axis
+        if (bvh_leaf_before_bins(count, depth)) return leaf(first, count, lo, hi);
+        // SAH over kBvhBins bins per axis
         float kk[3];
         bool use[3];
         for (int a = 0; a < 3; ++a) {
             float ext = chi[a] - clo[a];
             use[a] = ext > 0.0f;
-            kk[a] = use[a] ? (float)kBins / ext : 0.0f;
+            kk[a] = use[a] ? (float)kBvhBins / ext : 0.0f;
         }
         Bins bins;
         Bins *all = &bins;
@@ -487,48 +473,17 @@ struct Builder {
         } else {
             bin(first, first + count, clo, kk, use, *all);
         }
-        float best_cost = INFINITY;
-        int best_axis = -1, best_bin = 0;
-        for (int a = 0; a < 3; ++a) {
-            if (!use[a]) continue;
-            auto &bl = all->bl[a];
-            auto &bh = all->bh[a];
-            auto &bc = all->bc[a];
-            float rarea[kBins];
-            uint32_t rcount[kBins];
-            float rl[3] = {INFINITY, INFINITY, INFINITY}, rh[3] = {-INFINITY, -INFINITY, -INFINITY};
-            uint32_t rc = 0;
-            for (int b = kBins - 1; b > 0; --b) {
-                rc += bc[b];
-                for (int j = 0; j < 3; ++j) { rl[j] = std::min(rl[j], bl[b][j]); rh[j] = std::max(rh[j], bh[b][j]); }
-                rarea[b] = half_area(rl, rh);
-                rcount[b] = rc;
-            }
-            float ll[3] = {INFINITY, INFINITY, INFINITY}, lh[3] = {-INFINITY, -INFINITY, -INFINITY};
-            uint32_t lc = 0;
-            for (int b = 0; b < kBins - 1; ++b) {
-                lc += bc[b];
-                for (int j = 0; j < 3; ++j) { ll[j] = std::min(ll[j], bl[b][j]); lh[j] = std::max(lh[j], bh[b][j]); }
-                if (!lc || !rcount[b + 1]) continue;
-                float c = half_area(ll, lh) * (float)lc + rarea[b + 1] * (float)rcount[b + 1];
-                if (c < best_cost) { best_cost = c; best_axis = a; best_bin = b; }
-            }
-        }
-        float parent_area = half_area(lo, hi);
-        float leaf_cost = (float)count;
-        float split_cost = kNodeCost + (parent_area > 0.0f ? best_cost / parent_area : (float)count);
+        float best_cost;
+        int best_axis, best_bin;
+        bvh_best_split(*all, use, best_cost, best_axis, best_bin);
+        BvhSplit how = bvh_decide(count, depth, lo, hi, best_cost, best_axis);
+        if (how == kBvhLeaf) return leaf(first, count, lo, hi);
         uint32_t mid;
-        if (best_axis < 0 || depth >= kMaxDepth) {
-            if (count <= kMaxLeaf) return leaf(first, count, lo, hi);
-            mid = first + count / 2;  // coincident centroids: split by index
+        if (how == kBvhByIndex) {
+            mid = first + count / 2;  // coincident centroids (or the depth cap): split by index
         } else {
-            if (count <= kMaxLeaf && leaf_cost <= split_cost) return leaf(first, count, lo, hi);
-            float ext = chi[best_axis] - clo[best_axis];
-            float k = (float)kBins / ext;
-            auto left = [&](uint32_t i) {
-                int b = std::min(kBins - 1, (int)((prims[i].c[best_axis] - clo[best_axis]) * k));
-                return b <= best_bin;
-            };
+            float k = kk[best_axis];
+            auto left = [&](uint32_t i) { return bvh_bin(prims[i].c[best_axis], clo[best_axis], k) <= best_bin; };
             if (wide > 1) {
                 // stable partition by chunks: count, place through a scratch array, copy back
                 std::vector<uint32_t> lefts(wide, 0), starts(wide, 0);
@@ -562,7 +517,7 @@ struct Builder {
                 std::copy(tmp.begin(), tmp.end(), idx.begin() + first);
                 mid = first + total_left;
             } else {
-                auto it = std::partition(idx.begin() + first, idx.begin() + first + count, left);
+                auto it = std::stable_partition(idx.begin() + first, idx.begin() + first + count, left);
                 mid = (uint32_t)(it - idx.begin());
             }
             if (mid == first || mid == first + count) mid = first + count / 2;
@@ -599,17 +554,6 @@ struct Builder {
     }
 };
 
-// Boxes are padded so that culling stays conservative with respect to the triangle test's own
-// rounding: an absolute margin scaled by the coordinate magnitude.
-void pad_box(float lo[3], float hi[3]) {
-    for (int a = 0; a < 3; ++a) {
-        float m = std::max(std::fabs(lo[a]), std::fabs(hi[a]));
-        float pad = 1e-5f * std::max(1.0f, m);
-        lo[a] -= pad;
-        hi[a] += pad;
-    }
-}
-
 }  // namespace
 
 void build_bvh(HostScene &s) {
@@ -644,38 +588,34 @@ void build_bvh(HostScene &s) {
     std::iota(b.idx.begin(), b.idx.end(), 0u);
     std::vector<BvhNode> nodes;
     nodes.reserve(n);
-    nodes.push_back(BvhNode{});  // root placeholder
     uint32_t max_depth = 0;
+    // nodes in depth-first order, the root first, each left subtree before its right one
     Ref root = b.build(nodes, 0, (uint32_t)n, 1, max_depth);
     if (root.ref < 0) {
         // the whole set is one leaf: the root holds it and an empty second child
+        nodes.push_back(BvhNode{});
         BvhNode &r = nodes[0];
         r.c0[0] = root.lo[0]; r.c0[1] = root.hi[0]; r.c0[2] = root.lo[1]; r.c0[3] = root.hi[1];
         r.c2[0] = root.lo[2]; r.c2[1] = root.hi[2];
         r.c1[0] = 1e30f; r.c1[1] = -1e30f; r.c1[2] = 1e30f; r.c1[3] = -1e30f;
         r.c2[2] = 1e30f; r.c2[3] = -1e30f;
         r.ref[0] = root.ref; r.ref[1] = ~0; r.count[0] = 0; r.count[1] = 0;
-    } else {
-        // move the built root (index root.ref) into slot 0
-        nodes[0] = nodes[(size_t)root.ref];
-        for (auto &nd : nodes)
-            for (int c = 0; c < 2; ++c)
-                if (nd.ref[c] == root.ref) nd.ref[c] = 0;
     }
     for (auto &nd : nodes) {
         float lo[3] = {nd.c0[0], nd.c0[2], nd.c2[0]}, hi[3] = {nd.c0[1], nd.c0[3], nd.c2[1]};
         if (nd.ref[0] != ~0) {
-            pad_box(lo, hi);
+            bvh_pad_box(lo, hi);
             nd.c0[0] = lo[0]; nd.c0[1] = hi[0]; nd.c0[2] = lo[1]; nd.c0[3] = hi[1]; nd.c2[0] = lo[2]; nd.c2[1] = hi[2];
         }
         float lo1[3] = {nd.c1[0], nd.c1[2], nd.c2[2]}, hi1[3] = {nd.c1[1], nd.c1[3], nd.c2[3]};
         if (nd.ref[1] != ~0) {
-            pad_box(lo1, hi1);
+            bvh_pad_box(lo1, hi1);
             nd.c1[0] = lo1[0]; nd.c1[1] = hi1[0]; nd.c1[2] = lo1[1]; nd.c1[3] = hi1[1]; nd.c2[2] = lo1[2]; nd.c2[3] = hi1[2];
         }
     }
     s.nodes = std::move(nodes);
     s.bvh_depth = max_depth;
+    s.bvh_node_count = (uint32_t)s.nodes.size();
     par_chunks(0, (uint32_t)n, wide, [&](uint32_t lo_k, uint32_t hi_k, unsigned) {
         for (size_t k = lo_k; k < hi_k; ++k) {
             uint32_t i = b.idx[k];

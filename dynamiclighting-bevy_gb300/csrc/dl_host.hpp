@@ -73,13 +73,16 @@ struct HostScene {
     std::vector<BvhNode> nodes;
     std::vector<float> tri_v0, tri_e1, tri_e2;  // 4 floats each (w of v0: occluder index bits)
     uint32_t bvh_depth = 0;
+    uint32_t bvh_node_count = 0;  // inner nodes, from either builder (the device one fills no vectors)
 };
 
 // Validates, sorts and prepares (src/bake/baker.rs:32-75). Returns DL_OK or the error status
 // with `err` set to the reference's message.
 dl_status prepare_scene(const dl_bake_input &in, const dl_bake_options &o, HostScene &s, std::string &err);
 
-// Builds the occluder BVH (binned SAH, leaves of at most 4 triangles, depth capped at 60).
+// Builds the occluder BVH on the host (binned SAH, leaves of at most 4 triangles, depth capped at
+// 60; the rules of dl_bvh_rules.hpp). The bake builds the same tree on the device (dl_bvh.cu)
+// unless dl_bake_config.host_bvh asks for this one.
 void build_bvh(HostScene &s);
 
 // The first n = 2^m points of the sky's low-discrepancy sequence (src/bake/spread.rs:16-24) form

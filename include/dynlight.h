@@ -170,7 +170,9 @@ typedef struct dl_bake_config {
     uint32_t no_autotune;      /* 1: never time candidate launch shapes; unset knobs take defaults.
                                   0: knobs left 0 are picked by timing trials on the first run of a
                                   scene shape (cached per process) */
-    uint32_t reserved[5];
+    uint32_t host_bvh;         /* 1: build the occluder BVH on the host's cores and upload it;
+                                  0: build it on the device (the same tree, in milliseconds) */
+    uint32_t reserved[4];
 } dl_bake_config;
 
 /* Timings (device events, milliseconds) and counters of the last bake. */
@@ -343,6 +345,15 @@ dl_status dl_session_report(const dl_session *session, dl_bake_report *report);
  * dl_encode_payload on dl_session_result's scene. `*bytes` is freed with dl_free; the gzip
  * layer stays with the caller. */
 dl_status dl_session_encode_payload(dl_session *session, uint8_t **bytes, uint64_t *length, uint32_t *crc);
+/* No counterpart in the reference (whose occluder BVH is internal to Occluders,
+   src/bake/occluder.rs:63-114): a copy of the session's occluder BVH as the traversal reads it —
+   up to `node_cap` 64-byte nodes (child boxes c0, c1, c2 as 12 floats, then the two child
+   references as int32: >= 0 an inner node, < 0 a leaf ~(first << 3 | count), ~0 empty, then two
+   zero words) and up to `tri_cap` triangles in leaf order (12 floats: v0 with the occluder index's
+   bits in the fourth, e1 and e2 with a zero fourth). `*node_count` and `*depth` (the deepest
+   level, the root being 1) are set either way. For tests and tools. */
+dl_status dl_session_occluder_bvh(dl_session *session, void *nodes, uint64_t node_cap, float *triangles,
+                                  uint64_t tri_cap, uint32_t *node_count, uint32_t *depth);
 /* No counterpart in the reference (whose BounceMap is internal to bake_mesh_bounce,
    src/bake/bounce.rs:155-217): the last run's filtered bounce map of (mesh id, light slot) —
    its window (min_x, min_y, max_x, max_y) and up to `cap` RGB texels row-major over the window,
