@@ -568,8 +568,12 @@ struct BounceArgs {
 // the sum is the reference's sequential one for any group size. Sun gathers with a power-of-two
 // sample count up to `buffered` instead take their samples in the coherent order of the sample
 // net (sample_order: a group's lanes send nearby directions together), buffer every sample's
-// contribution and let the leader add them in sample order at the end. Dynamic shared memory
-// holds the traversal stacks, one float4 contribution slot per thread and the groups' buffers. MINB is the launch bound's
+// contribution and let the leader add them in sample order at the end. Their shadow rays wait:
+// a sample whose hit faces the sun queues its shadow ray's origin (up to buffered / 4 of them per
+// group, the rest are traced at once), and the group traces the queue after the closest-hit
+// rounds, W at a time, instead of holding every round for the few lanes that have one. Dynamic
+// shared memory holds the traversal stacks, one float4 contribution slot per thread, the groups'
+// buffers and their shadow-ray queues. MINB is the launch bound's
 // blocks per SM (the register budget: 6 leaves the compiler its 80 registers, 8 asks for 64).
 template <bool REFINE, int MINB>
 __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs a) {
@@ -577,8 +581,11 @@ __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs
     int *my = smem + threadIdx.x;
     float4 *part = reinterpret_cast<float4 *>(smem + (size_t)a.stack_depth * kBlock);
     const uint32_t lane = lane_id(), W = a.lanes, sub = lane % W, per_step = 32 / W;
-    // this lane group's buffer of `buffered` contributions
-    float4 *buf = part + kBlock + (size_t)((threadIdx.x >> 5) * per_step + lane / W) * a.buffered;
+    // this lane group's buffer of `buffered` contributions and queue of `queued` shadow rays
+    const uint32_t group = (threadIdx.x >> 5) * per_step + lane / W, queued = a.buffered / 4;
+    float4 *buf = part + kBlock + (size_t)group * a.buffered;
+    float4 *queue = part + kBlock + (size_t)(kBlock / W) * a.buffered + (size_t)group * queued;
+    const unsigned group_lanes = W == 32 ? 0xFFFFFFFFu : ((1u << W) - 1u) << (lane / W * W);
     unsigned long long rays = 0;
     Visits vis{0, 0, 0};
     for (;;) {
@@ -624,11 +631,28 @@ __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs
         const uint16_t *order = sun && samples <= a.buffered ? sample_order(sc, samples) : nullptr;
         FSum3<REFINE> sum;
         const uint32_t rounds = __reduce_max_sync(0xFFFFFFFFu, (samples + W - 1) / W);
+        uint32_t waiting = 0;  // the group's queued shadow rays
         for (uint32_t r = 0; r < rounds; ++r) {
             uint32_t k = r * W + sub;
             uint32_t i = order && k < samples ? order[k] : k;
             Contribution c{f3{0.0f, 0.0f, 0.0f}, false, 0};
-            if (i < samples) {
+            SunHit h{f3{0.0f, 0.0f, 0.0f}, f3{0.0f, 0.0f, 0.0f}, false};
+            if (order && i < samples) {
+                h = sun_hit<REFINE>(sc, sc.lights[s], origin, normal, sg, i, my, kBlock, &vis);
+                rays += h.pending ? 2 : 1;
+            }
+            const unsigned pend = __ballot_sync(0xFFFFFFFFu, h.pending) & group_lanes;
+            if (order) {
+                uint32_t slot = waiting + __popc(pend & ((1u << lane) - 1u));
+                bool open = false;
+                if (h.pending && slot < queued) {
+                    queue[slot] = make_float4(h.point.x, h.point.y, h.point.z, __uint_as_float(i));
+                } else if (h.pending) {
+                    open = sun_open<REFINE>(sc, sc.lights[s], h.point, my, kBlock, &vis);
+                }
+                if (i < samples) buf[i] = make_float4(h.value.x, h.value.y, h.value.z, open ? 1.0f : 0.0f);
+                waiting = min(queued, waiting + __popc(pend));
+            } else if (i < samples) {
                 const DevLight &l = sc.lights[s];
                 if (sun) {
                     c = sun_sample<REFINE>(sc, l, origin, normal, sg, i, my, kBlock, &vis);
@@ -639,12 +663,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs
                 }
                 rays += c.rays;
             }
-            float4 cv = make_float4(c.value.x, c.value.y, c.value.z, c.add ? 1.0f : 0.0f);
-            if (order) {
-                if (i < samples) buf[i] = cv;
-            } else {
-                part[threadIdx.x] = cv;
-            }
+            if (!order) part[threadIdx.x] = make_float4(c.value.x, c.value.y, c.value.z, c.add ? 1.0f : 0.0f);
             __syncwarp();
             if (!order && sub == 0 && samples) {
                 for (uint32_t j = 0; j < W && r * W + j < samples; ++j) {
@@ -654,6 +673,15 @@ __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs
             }
             __syncwarp();
         }
+        if (order) {
+            // the queued shadow rays, W at a time
+            for (uint32_t q = sub; q < waiting; q += W) {
+                float4 e = queue[q];
+                if (sun_open<REFINE>(sc, sc.lights[s], f3{e.x, e.y, e.z}, my, kBlock, &vis))
+                    buf[__float_as_uint(e.w)].w = 1.0f;
+            }
+        }
+        __syncwarp();
         if (order && sub == 0) {
             for (uint32_t j = 0; j < samples; ++j) {
                 float4 q = buf[j];
@@ -1878,15 +1906,19 @@ struct GatherTune {
     double ms = 0.0;
 };
 using GatherKernel = void (*)(DevScene, BounceArgs);
+// The gather kernel of a variant, allowed kGatherSmemMax bytes of dynamic shared memory (above
+// the default 48 KB: 16-lane groups of 256 buffered samples need 74 KB with a 64-entry stack).
+constexpr int kGatherSmemMax = 80 * 1024;
 GatherKernel gather_kernel(bool refine, uint32_t minb) {
-    if (refine) return k_gather<true, 6>;
-    return minb == 8 ? k_gather<false, 8> : k_gather<false, 6>;
+    GatherKernel k = refine ? k_gather<true, 6> : minb == 8 ? k_gather<false, 8> : k_gather<false, 6>;
+    CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kGatherSmemMax));
+    return k;
 }
 // Shared memory of a gather launch: stacks, the round slots and, for the coherent order, a
-// buffer of `buffered` contributions per lane group.
+// buffer of `buffered` contributions and a queue of buffered / 4 shadow rays per lane group.
 size_t gather_smem(uint32_t depth, uint32_t lanes, uint32_t buffered) {
     return (size_t)depth * kBlock * sizeof(int) + kBlock * sizeof(float4) +
-           (size_t)(kBlock / lanes) * buffered * sizeof(float4);
+           (size_t)(kBlock / lanes) * (buffered + buffered / 4) * sizeof(float4);
 }
 // The buffer for coherent sun gathers: the largest power-of-two sun bounce sample count up to
 // 256, for groups of 16 or 32 lanes (0 otherwise).
