@@ -6,9 +6,11 @@
 //   dot(a, b) = (a.x*b.x + a.y*b.y) + a.z*b.z
 //   cross(a, b) = (a.y*b.z - b.y*a.z, a.z*b.x - b.z*a.x, a.x*b.y - b.x*a.y)
 //   normalize(v) = v * (1 / sqrt(dot(v, v)))
-// Transcendentals of f32 arguments are evaluated in binary64 (Cody–Waite reduction by pi/2 and
-// Taylor series) and rounded once, so host and device agree bit for bit and the result is the
-// correctly rounded f32 except for ~1e-8 of arguments.
+// Transcendentals of f32 arguments: the binary64 evaluation (Cody–Waite reduction by pi/2 and
+// Taylor series, rounded once) is the definition host and device share. On the device, sin/cos
+// and acos first run in double-float binary32 arithmetic (error-free sums and products, Dekker
+// 1971) to about 2^-40 and keep that result only when Ziv's rounding test shows it rounds to the
+// same binary32 as the exact value; otherwise the binary64 path decides, so both give one answer.
 #pragma once
 
 #include <cstdint>
