@@ -427,8 +427,13 @@ __global__ void __launch_bounds__(kBlock, MINB) k_trace_batched(DevScene sc, Tra
                     off.y = rng.next_f32();
                     f3 side, across;
                     ortho_pair(nrm, side, across);
-                    for (uint32_t k = sub; k < sc.sky_samples; k += W) {
-                        uint32_t j = sc.sky_order ? sc.sky_order[k] : k;
+                    // in the shift-aligned coherent order when the sample count allows it: the
+                    // warp's texels (neighbours) then trace their rank-k rays in about one direction
+                    const uint32_t n = sc.sky_samples;
+                    const bool aligned = n >= 16 && n <= kMaxOrdered && !(n & (n - 1));
+                    const uint32_t shift = aligned ? net_shift(n, off) : 0u;
+                    for (uint32_t k = sub; k < n; k += W) {
+                        uint32_t j = aligned ? shifted_sample(sc, n, shift, k) : sc.sky_order ? sc.sky_order[k] : k;
                         if (!tr(cosine_direction_basis(nrm, side, across, spread(j, off, true)), INFINITY)) ++open;
                     }
                 }
@@ -1756,11 +1761,16 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     sc.area_samples = o->area_light_samples;
     sc.area_min_samples = o->area_light_min_samples;
     sc.sky_samples = o->sky_samples;
-    std::vector<uint16_t> orders;
+    std::vector<uint16_t> orders, cells, cell_samples;
     for (uint32_t n = 16; n <= kMaxOrdered; n *= 2) {
         std::vector<uint16_t> o16 = sky_sample_order(n);
         orders.insert(orders.end(), o16.begin(), o16.end());
+        SampleCells c = sample_cells(n);
+        cells.insert(cells.end(), c.cells.begin(), c.cells.end());
+        cell_samples.insert(cell_samples.end(), c.samples.begin(), c.samples.end());
     }
+    up(cells.data(), cells.size() * 2, sc.order_cells);
+    up(cell_samples.data(), cell_samples.size() * 2, sc.cell_samples);
     std::vector<uint16_t> sky_order = sky_sample_order(o->sky_samples);
     up(orders.data(), orders.size() * 2, sc.orders);
     sc.sky_order = nullptr;

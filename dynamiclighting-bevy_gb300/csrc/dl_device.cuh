@@ -49,11 +49,31 @@ struct DevScene {
     // (the table of n starts at n - 16); sky_order is the sky's, or null
     const uint16_t *orders;
     const uint16_t *sky_order;
+    // sample_cells (dl_host.hpp) for the same n, laid out like `orders`
+    const uint16_t *order_cells, *cell_samples;
 };
 constexpr uint32_t kMaxOrdered = 4096;
 // The coherent order of n samples, or null when n is not a power of two from 16 to kMaxOrdered.
 __device__ __forceinline__ const uint16_t *sample_order(const DevScene &sc, uint32_t n) {
     return (n >= 16 && n <= kMaxOrdered && !(n & (n - 1))) ? sc.orders + (n - 16) : nullptr;
+}
+// The shift of a net of n samples (n a power of two from 16 to kMaxOrdered) by `off` in whole
+// cells, packed as x | y << 8 | xbits << 16 | ybits << 24.
+__device__ __forceinline__ uint32_t net_shift(uint32_t n, f2 off) {
+    uint32_t m = 31 - __clz(n), xb = (m + 1) / 2, yb = m / 2;
+    uint32_t sx = min((1u << xb) - 1, (uint32_t)(off.x * (float)(1u << xb)));
+    uint32_t sy = min((1u << yb) - 1, (uint32_t)(off.y * (float)(1u << yb)));
+    return sx | sy << 8 | xb << 16 | yb << 24;
+}
+// Sample of rank k of a net of n samples shifted by `shift` (net_shift): the point of the cell of
+// rank k moved back by the shift, so that texels with different shifts send their rank-k rays in
+// about the same direction. A permutation of 0 .. n-1 over k.
+__device__ __forceinline__ uint32_t shifted_sample(const DevScene &sc, uint32_t n, uint32_t shift, uint32_t k) {
+    const uint32_t c = sc.order_cells[n - 16 + k];
+    const uint32_t xb = (shift >> 16) & 0xFFu, yb = shift >> 24;
+    const uint32_t cx = ((c & 0xFFu) - (shift & 0xFFu)) & ((1u << xb) - 1u);
+    const uint32_t cy = ((c >> 8) - ((shift >> 8) & 0xFFu)) & ((1u << yb) - 1u);
+    return sc.cell_samples[n - 16 + (cy << xb | cx)];
 }
 enum : uint32_t { kMeshNormals = 1, kMeshOccludes = 2, kMeshAlpha = 4 };
 

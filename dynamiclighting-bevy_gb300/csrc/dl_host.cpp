@@ -675,6 +675,24 @@ std::vector<uint16_t> sky_sample_order(uint32_t n) {
     return order;
 }
 
+SampleCells sample_cells(uint32_t n) {
+    SampleCells c;
+    std::vector<uint16_t> order = sky_sample_order(n);
+    if (order.empty()) return c;
+    uint32_t m = 0;
+    while ((1u << m) < n) ++m;
+    const uint32_t xbits = (m + 1) / 2, ybits = m / 2;
+    c.cells.resize(n);
+    c.samples.resize(n);
+    for (uint32_t r = 0; r < n; ++r) {
+        uint32_t j = order[r];
+        uint32_t cx = rev_bits(j) >> (32 - xbits), cy = ybits ? sobol2(j) >> (32 - ybits) : 0u;
+        c.cells[r] = (uint16_t)(cx | cy << 8);
+        c.samples[cy << xbits | cx] = (uint16_t)j;
+    }
+    return c;
+}
+
 // ---- maps for moving meshes: host halves -------------------------------------------------------
 
 // Calls f(vertex) for every corner of every occluder triangle (sun_map.rs:164-170).

@@ -92,6 +92,17 @@ void build_bvh(HostScene &s);
 // open count of a sky texel does not depend on the order its samples are traced in. Empty
 // unless n is a power of two from 16 to 65536.
 std::vector<uint16_t> sky_sample_order(uint32_t n);
+// The same net's cells for a shifted net: `cells[r]` is the cell (x | y << 8) of the r-th entry of
+// sky_sample_order(n) and `samples[y << xbits | x]` the one point of cell (x, y), where the grid
+// is 2^xbits x 2^ybits, xbits = ceil(m / 2). A texel whose net is shifted by `off`
+// (spread.rs:16-24, a toroidal shift) takes rank r from the cell of rank r moved back by the shift's
+// whole cells, floor(off * grid): its shifted point then lies in that cell or the next, so every
+// texel's r-th ray leaves in about the same direction. Empty unless n is a power of two from 16 to
+// 65536.
+struct SampleCells {
+    std::vector<uint16_t> cells, samples;
+};
+SampleCells sample_cells(uint32_t n);
 
 // A sun map's frame and bounds (src/bake/sun_map.rs:25-45,83-161): `empty` when there is no
 // static geometry (one texel that nothing is behind).

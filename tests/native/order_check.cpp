@@ -1,6 +1,6 @@
 // The coherent sky sample order (dl_host.cpp): a permutation of 0 .. n-1 whose consecutive
-// groups of 16 fall in one 4 x 4 block of the (0, m, 2)-net's cells. Built and run by
-// tests/test_math_paths.py.
+// groups of 16 fall in one 4 x 4 block of the (0, m, 2)-net's cells; and its shift-aligned form
+// (sample_cells). Built and run by tests/test_math_paths.py.
 #include <cstdio>
 #include <vector>
 
@@ -28,6 +28,39 @@ int main() {
         }
     }
     failures += !dl::sky_sample_order(100).empty() + !dl::sky_sample_order(8).empty();
+    // the shift-aligned order (dl::sample_cells, used as the device's shifted_sample): for any
+    // shift a permutation, rank r's shifted point in cell r or the next on each axis
+    uint64_t state = 0x9E3779B97F4A7C15ull;
+    auto next_unit = [&state] {
+        state = state * 6364136223846793005ull + 1442695040888963407ull;
+        return (float)(uint32_t)(state >> 40) * (1.0f / 16777216.0f);
+    };
+    for (uint32_t n : {16u, 32u, 128u, 256u, 2048u, 4096u}) {
+        dl::SampleCells c = dl::sample_cells(n);
+        uint32_t m = 0;
+        while ((1u << m) < n) ++m;
+        const uint32_t xb = (m + 1) / 2, yb = m / 2, nx = 1u << xb, ny = 1u << yb;
+        std::vector<int> cell_seen(n, 0);
+        for (uint16_t j : c.samples) ++cell_seen[j];
+        for (uint32_t j = 0; j < n; ++j) failures += cell_seen[j] != 1;
+        for (int trial = 0; trial < 64; ++trial) {
+            float ox = trial == 0 ? 0.0f : next_unit(), oy = trial == 0 ? 0.999999f : next_unit();
+            uint32_t sx = (uint32_t)(ox * (float)nx), sy = (uint32_t)(oy * (float)ny);
+            sx = sx < nx - 1 ? sx : nx - 1;
+            sy = sy < ny - 1 ? sy : ny - 1;
+            std::vector<int> seen(n, 0);
+            for (uint32_t r = 0; r < n; ++r) {
+                uint32_t cx = c.cells[r] & 0xFFu, cy = c.cells[r] >> 8;
+                uint32_t j = c.samples[((cy - sy) & (ny - 1)) << xb | ((cx - sx) & (nx - 1))];
+                ++seen[j];
+                dl::f2 p = dl::spread(j, dl::f2{ox, oy}, true);
+                uint32_t px = (uint32_t)(p.x * (float)nx), py = (uint32_t)(p.y * (float)ny);
+                failures += ((px - cx) & (nx - 1)) > 1 || ((py - cy) & (ny - 1)) > 1;
+            }
+            for (uint32_t j = 0; j < n; ++j) failures += seen[j] != 1;
+        }
+    }
+    failures += !dl::sample_cells(100).cells.empty();
     std::printf("order failures %d\n", failures);
     return failures ? 1 : 0;
 }
