@@ -563,34 +563,40 @@ struct BounceArgs {
     uint32_t lanes;         // lanes sharing one texel's samples (1, 2, 4, 8, 16 or 32)
     uint32_t sample_every;  // tuning trials: one claimed step in `sample_every` (1: all)
     uint32_t stack_depth;   // shared-memory stack entries per thread
-    uint32_t buffered;      // samples each lane group can buffer for the coherent order (0: none)
+    uint32_t buffered;      // sun samples a lane group can hold for the aligned order (0: none)
+    float4 *scratch;        // per lane group (blockIdx * groups + group): 2 * buffered float4
     unsigned long long *head;  // steps claimed so far (32 / lanes items per step)
 };
 
 // gather_triangle / gather_sun (bounce.rs:235-292, sun_bounce.rs:24-80): a group of `lanes`
 // lanes per (bounce pair, texel) item. Each round, lane k of a group evaluates sample
 // round * lanes + k; the group leader then adds the round's contributions in sample order, so
-// the sum is the reference's sequential one for any group size. Sun gathers with a power-of-two
-// sample count up to `buffered` instead take their samples in the coherent order of the sample
-// net (sample_order: a group's lanes send nearby directions together), buffer every sample's
-// contribution and let the leader add them in sample order at the end. Their shadow rays wait:
-// a sample whose hit faces the sun queues its shadow ray's origin (up to buffered / 4 of them per
-// group, the rest are traced at once), and the group traces the queue after the closest-hit
-// rounds, W at a time, instead of holding every round for the few lanes that have one. Dynamic
-// shared memory holds the traversal stacks, one float4 contribution slot per thread, the groups'
-// buffers and their shadow-ray queues. MINB is the launch bound's
-// blocks per SM (the register budget: 6 leaves the compiler its 80 registers, 8 asks for 64).
+// the sum is the reference's sequential one for any group size.
+// Sun gathers with a power-of-two sample count up to `buffered` take their samples in the
+// shift-aligned coherent order instead (shifted_sample): round r of every group in the warp
+// traces ranks r * lanes + k, so the warp's texels (neighbours along a triangle) send their rays
+// in about the same directions. A sample whose closest hit faces the sun and is lit by it
+// stores its value and its shadow ray's origin in the group's scratch (global memory, indexed
+// by sample) and sets its bit in the group's mask (shared memory); after the closest-hit rounds
+// the group traces those shadow rays together, W at a time (parallel rays towards the sun),
+// clearing the bits of blocked ones, and the leader adds the values left in the mask in sample
+// order. Dynamic shared memory holds the traversal stacks, one float4 contribution slot per
+// thread and the groups' masks. MINB is the launch bound's blocks per SM (the register budget: 6 leaves the compiler its 80 registers, 8 asks for 64).
 template <bool REFINE, int MINB>
 __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs a) {
     extern __shared__ int smem[];
     int *my = smem + threadIdx.x;
     float4 *part = reinterpret_cast<float4 *>(smem + (size_t)a.stack_depth * kBlock);
     const uint32_t lane = lane_id(), W = a.lanes, sub = lane % W, per_step = 32 / W;
-    // this lane group's buffer of `buffered` contributions and queue of `queued` shadow rays
-    const uint32_t group = (threadIdx.x >> 5) * per_step + lane / W, queued = a.buffered / 4;
-    float4 *buf = part + kBlock + (size_t)group * a.buffered;
-    float4 *queue = part + kBlock + (size_t)(kBlock / W) * a.buffered + (size_t)group * queued;
+    // this lane group's masks (shared memory: samples whose hit is lit, then those whose shadow
+    // ray is blocked) and scratch (global memory) for aligned sun gathers
+    const uint32_t group = (threadIdx.x >> 5) * per_step + lane / W, words = a.buffered / 32;
     const unsigned group_lanes = W == 32 ? 0xFFFFFFFFu : ((1u << W) - 1u) << (lane / W * W);
+    uint32_t *lit = reinterpret_cast<uint32_t *>(part + kBlock) + (size_t)group * 2 * words;
+    uint32_t *blocked = lit + words;
+    float4 *scratch = a.scratch + ((size_t)blockIdx.x * (kBlock / W) + group) * 2 * a.buffered;
+    for (uint32_t w = sub; w < 2 * words; w += W) lit[w] = 0u;
+    __syncwarp();
     unsigned long long rays = 0;
     Visits vis{0, 0, 0};
     for (;;) {
@@ -633,64 +639,76 @@ __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs
             }
         }
         if (!active) samples = 0;
-        const uint16_t *order = sun && samples <= a.buffered ? sample_order(sc, samples) : nullptr;
+        const bool aligned = sun && samples >= 32 && samples <= a.buffered && !(samples & (samples - 1));
+        const uint32_t shift = aligned ? net_shift(samples, sg.off) : 0u;
         FSum3<REFINE> sum;
         const uint32_t rounds = __reduce_max_sync(0xFFFFFFFFu, (samples + W - 1) / W);
-        uint32_t waiting = 0;  // the group's queued shadow rays
         for (uint32_t r = 0; r < rounds; ++r) {
-            uint32_t k = r * W + sub;
-            uint32_t i = order && k < samples ? order[k] : k;
-            Contribution c{f3{0.0f, 0.0f, 0.0f}, false, 0};
-            SunHit h{f3{0.0f, 0.0f, 0.0f}, f3{0.0f, 0.0f, 0.0f}, false};
-            if (order && i < samples) {
-                h = sun_hit<REFINE>(sc, sc.lights[s], origin, normal, sg, i, my, kBlock, &vis);
-                rays += h.pending ? 2 : 1;
-            }
-            const unsigned pend = __ballot_sync(0xFFFFFFFFu, h.pending) & group_lanes;
-            if (order) {
-                uint32_t slot = waiting + __popc(pend & ((1u << lane) - 1u));
-                bool open = false;
-                if (h.pending && slot < queued) {
-                    queue[slot] = make_float4(h.point.x, h.point.y, h.point.z, __uint_as_float(i));
-                } else if (h.pending) {
-                    open = sun_open<REFINE>(sc, sc.lights[s], h.point, my, kBlock, &vis);
+            const uint32_t k = r * W + sub;
+            if (aligned) {
+                if (k < samples) {
+                    const uint32_t i = shifted_sample(sc, samples, shift, k);
+                    SunHit h = sun_hit<REFINE>(sc, sc.lights[s], origin, normal, sg, i, my, kBlock, &vis);
+                    rays += h.pending ? 2 : 1;
+                    if (h.pending) {
+                        scratch[2 * i] = make_float4(h.value.x, h.value.y, h.value.z, 0.0f);
+                        scratch[2 * i + 1] = make_float4(h.point.x, h.point.y, h.point.z, 0.0f);
+                        atomicOr(&lit[i >> 5], 1u << (i & 31u));
+                    }
                 }
-                if (i < samples) buf[i] = make_float4(h.value.x, h.value.y, h.value.z, open ? 1.0f : 0.0f);
-                waiting = min(queued, waiting + __popc(pend));
-            } else if (i < samples) {
+                continue;  // no per-round sum: the group syncs below use group masks
+            }
+            Contribution c{f3{0.0f, 0.0f, 0.0f}, false, 0};
+            if (k < samples) {
                 const DevLight &l = sc.lights[s];
                 if (sun) {
-                    c = sun_sample<REFINE>(sc, l, origin, normal, sg, i, my, kBlock, &vis);
+                    c = sun_sample<REFINE>(sc, l, origin, normal, sg, k, my, kBlock, &vis);
                 } else {
                     Tracer<false, REFINE> tr{sc, origin, (l.flags & kLightAlpha) != 0, my, kBlock, &vis};
-                    c = local_sample(sc, l, a.photons + (size_t)l.cube * 6 * a.res * a.res, a.res, normal, lg, i, tr);
-                    lg.rng.advance(2ull * (W - 1));  // to the lane's next sample, i + W
+                    c = local_sample(sc, l, a.photons + (size_t)l.cube * 6 * a.res * a.res, a.res, normal, lg, k, tr);
+                    lg.rng.advance(2ull * (W - 1));  // to the lane's next sample, k + W
                 }
                 rays += c.rays;
             }
-            if (!order) part[threadIdx.x] = make_float4(c.value.x, c.value.y, c.value.z, c.add ? 1.0f : 0.0f);
-            __syncwarp();
-            if (!order && sub == 0 && samples) {
+            part[threadIdx.x] = make_float4(c.value.x, c.value.y, c.value.z, c.add ? 1.0f : 0.0f);
+            __syncwarp(group_lanes);
+            if (sub == 0 && samples) {
                 for (uint32_t j = 0; j < W && r * W + j < samples; ++j) {
                     float4 q = part[threadIdx.x + j];
                     if (q.w != 0.0f) sum.add(f3{q.x, q.y, q.z});
                 }
             }
-            __syncwarp();
+            __syncwarp(group_lanes);
         }
-        if (order) {
-            // the queued shadow rays, W at a time
-            for (uint32_t q = sub; q < waiting; q += W) {
-                float4 e = queue[q];
-                if (sun_open<REFINE>(sc, sc.lights[s], f3{e.x, e.y, e.z}, my, kBlock, &vis))
-                    buf[__float_as_uint(e.w)].w = 1.0f;
+        __syncwarp();
+        if (aligned) {
+            // the shadow rays of the lit hits, spread over the group's lanes in sample order
+            uint32_t nth = 0;
+            for (uint32_t w = 0; w < samples / 32; ++w) {
+                uint32_t bits = lit[w];  // read-only in this phase
+                while (bits) {
+                    const uint32_t b = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    if (nth++ % W != sub) continue;
+                    const uint32_t i = w * 32 + b;
+                    const float4 q = scratch[2 * i + 1];
+                    if (!sun_open<REFINE>(sc, sc.lights[s], f3{q.x, q.y, q.z}, my, kBlock, &vis))
+                        atomicOr(&blocked[w], 1u << b);
+                }
             }
         }
         __syncwarp();
-        if (order && sub == 0) {
-            for (uint32_t j = 0; j < samples; ++j) {
-                float4 q = buf[j];
-                if (q.w != 0.0f) sum.add(f3{q.x, q.y, q.z});
+        if (aligned && sub == 0) {
+            for (uint32_t w = 0; w < samples / 32; ++w) {
+                uint32_t bits = lit[w] & ~blocked[w];
+                while (bits) {
+                    const uint32_t b = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    const float4 q = scratch[2 * (w * 32 + b)];
+                    sum.add(f3{q.x, q.y, q.z});
+                }
+                lit[w] = 0u;
+                blocked[w] = 0u;
             }
         }
         __syncwarp();
@@ -1924,23 +1942,27 @@ GatherKernel gather_kernel(bool refine, uint32_t minb) {
     CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kGatherSmemMax));
     return k;
 }
-// Shared memory of a gather launch: stacks, the round slots and, for the coherent order, a
-// buffer of `buffered` contributions and a queue of buffered / 4 shadow rays per lane group.
+// Shared memory of a gather launch: stacks, the round slots and, for aligned sun gathers, two
+// masks of `buffered` bits per lane group.
 size_t gather_smem(uint32_t depth, uint32_t lanes, uint32_t buffered) {
     return (size_t)depth * kBlock * sizeof(int) + kBlock * sizeof(float4) +
-           (size_t)(kBlock / lanes) * (buffered + buffered / 4) * sizeof(float4);
+           (size_t)(kBlock / lanes) * 2 * (buffered / 32) * sizeof(uint32_t);
 }
-// The buffer for coherent sun gathers: the largest power-of-two sun bounce sample count up to
-// 256, for groups of 16 or 32 lanes (0 otherwise).
-uint32_t gather_buffer(const HostScene &h, uint32_t lanes) {
-    if (lanes < 16) return 0;
+// The samples a lane group holds for aligned sun gathers: the largest power-of-two sun bounce
+// sample count from 32 to 256 (0 when there is none).
+uint32_t gather_buffer(const HostScene &h, uint32_t) {
     uint32_t most = 0;
     for (const DevLight &l : h.lights)
         if (l.shape == DL_SHAPE_SUN && (l.flags & kLightBounce)) {
             uint32_t n = l.bounce_samples;
-            if (n >= 16 && n <= 256 && !(n & (n - 1))) most = std::max(most, n);
+            if (n >= 32 && n <= 256 && !(n & (n - 1))) most = std::max(most, n);
         }
     return most;
+}
+// The lane groups' scratch of a gather launch (2 float4 per held sample per group), from the
+// session's pool: the largest launch (one lane per group) sizes it once.
+float4 *gather_scratch(dl_session &s, uint32_t blocks, uint32_t lanes, uint32_t buffered) {
+    return s.pool.get<float4>("gather_scratch", (size_t)blocks * (kBlock / lanes) * 2 * buffered);
 }
 std::map<TuneKey, GatherTune> g_gather_cache;
 
@@ -1991,6 +2013,7 @@ GatherTune gather_tune(dl_session &s, BounceArgs ba, uint32_t bpairs, bool refin
             uint32_t blocks = blocks_for(minb, w);
             ba.lanes = w;
             ba.buffered = gather_buffer(s.host, w);
+            ba.scratch = gather_scratch(s, blocks, w, ba.buffered);
             CK(cudaMemsetAsync(ba.head, 0, sizeof(unsigned long long), st));
             CK(cudaEventRecord(a, st));
             gather_kernel(refine, minb)<<<blocks, kBlock, gather_smem(best.stack_depth, w, ba.buffered), st>>>(
@@ -2424,6 +2447,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
             ba.lanes = g.lanes;
             ba.stack_depth = g.stack_depth;
             ba.buffered = g.buffered;
+            ba.scratch = gather_scratch(s, g.blocks, g.lanes, g.buffered);
             s.report.tuned_gather_lanes = g.lanes;
             s.report.tune_trials += g.trials;
             s.report.ms_tune += g.ms;
