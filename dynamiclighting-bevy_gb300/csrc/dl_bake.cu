@@ -378,11 +378,12 @@ __device__ __forceinline__ unsigned long long claim(const TraceArgs &a, unsigned
 }
 
 // Batched form: persistent warps pull chunks of (pair, texel) items from one queue. Items are
-// ordered sky pairs first, then soft, then hard, so the longest work starts first. With
-// sky_lanes = W > 1 the sky items run first in a grouped phase: W lanes share one texel, each
-// tracing every W-th of its samples, and the open counts are summed across the group (an integer
-// sum, so the level is the same as one lane tracing them all in order). MINB is the launch bound's
-// blocks per SM (the register budget). The stack lives in dynamic shared memory.
+// ordered sky pairs first, then soft, then hard, so the longest work starts first. The sky items
+// run first in a grouped phase: W = sky_lanes lanes share one texel, each tracing every W-th rank
+// of its samples in the shift-aligned coherent order, and the open counts are summed across the
+// group (an integer sum, so the level is the same as one lane tracing them all in index order).
+// MINB is the launch bound's blocks per SM (the register budget). The stack lives in dynamic
+// shared memory.
 template <bool COUNT, bool REFINE, int MINB>
 __global__ void __launch_bounds__(kBlock, MINB) k_trace_batched(DevScene sc, TraceArgs a) {
     extern __shared__ int stack[];
@@ -393,7 +394,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_trace_batched(DevScene sc, Tra
     uint32_t grabs = 0;
     const uint32_t W = a.sky_lanes;
     unsigned long long first = 0;
-    if (W > 1 && a.sky_items) {
+    if (a.sky_items) {
         const uint32_t per_step = 32 / W, sub = lane % W;
         const unsigned long long end = a.sky_items;
         first = end;
@@ -1859,7 +1860,7 @@ TraceTune trace_tune(dl_session &s, TraceArgs ta, bool refine, bool count, dl_pr
     std::vector<uint32_t> grabs = c.chunk_texels ? std::vector<uint32_t>{std::max(1u, c.chunk_texels / 32)}
                                                  : std::vector<uint32_t>{1, 2};
     std::vector<uint32_t> lanes = c.sample_lanes ? std::vector<uint32_t>{c.sample_lanes}
-                                  : ta.sky_items  ? std::vector<uint32_t>{1, 4, 8, 16}
+                                  : ta.sky_items  ? std::vector<uint32_t>{1, 2, 4, 8, 16}
                                                   : std::vector<uint32_t>{1};
     std::vector<uint32_t> minbs = (count || refine) ? std::vector<uint32_t>{7} : std::vector<uint32_t>{7, 8};
     const uint32_t every = ta.items >= (4u << 20) ? 8 : ta.items >= (1u << 20) ? 4 : 0;
