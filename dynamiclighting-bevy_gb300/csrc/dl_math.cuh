@@ -248,21 +248,28 @@ DL_HD FF ff_neg(FF a) { return FF{-a.h, -a.l}; }
 // sin(r) and cos(r), |r| <= pi/4, r = rh + rl: Taylor coefficients as binary32 pairs (hi + lo =
 // (-1)^n/(2n+1)! or (-1)^n/(2n)! to 48 bits) for the leading terms, single binary32 for the tail
 // terms whose share of the result is below 2^-17.
-DL_HD void ff_sincos_poly(FF r, FF &s, FF &c) {
-    FF r2 = ff_mul(r, r);
+DL_HD FF ff_sin_poly(FF r, FF r2) {
     float z = r2.h;
     float ts = 2.7557318844628753e-06f + z * (-2.5052107943679403e-08f + z * (1.6059044372074283e-10f +
                                                                             z * -7.647163609812713e-13f));
     FF p = ff_add_f(FF{-0.00019841270113829523f, 2.725596874933456e-12f}, z * ts);
     p = ff_add(FF{0.008333333767950535f, -4.34617203337595e-10f}, ff_mul(r2, p));
     p = ff_add(FF{-0.1666666716337204f, 4.967053879312289e-09f}, ff_mul(r2, p));
-    s = ff_add(r, ff_mul(ff_mul(r, r2), p));
+    return ff_add(r, ff_mul(ff_mul(r, r2), p));
+}
+DL_HD FF ff_cos_poly(FF r2) {
+    float z = r2.h;
     float tc = 2.4801587642286904e-05f + z * (-2.755731998149713e-07f + z * (2.0876755879584152e-09f +
                                                                           z * -1.147074536050896e-11f));
     FF q = ff_add_f(FF{-0.0013888889225199819f, 3.3631094437103215e-11f}, z * tc);
     q = ff_add(FF{0.0416666679084301f, -1.2417634698280722e-09f}, ff_mul(r2, q));
     q = ff_add_f(ff_mul(r2, q), -0.5f);
-    c = ff_add_f(ff_mul(r2, q), 1.0f);
+    return ff_add_f(ff_mul(r2, q), 1.0f);
+}
+DL_HD void ff_sincos_poly(FF r, FF &s, FF &c) {
+    FF r2 = ff_mul(r, r);
+    s = ff_sin_poly(r, r2);
+    c = ff_cos_poly(r2);
 }
 // Ziv's rounding test: true when every value within 2^-36 relative of h + l rounds to h.
 DL_HD bool ff_rounds_to(FF v, float &out) {
@@ -315,10 +322,27 @@ DL_HD void sincos_f(float x, float &s, float &c) {
     s = (float)sd;
     c = (float)cd;
 }
+// sin alone: the reduction of sincos_f and only the polynomial the quadrant needs (sin of the
+// reduced argument for even quadrants, cos for odd ones), its own rounding test, the same
+// binary64 fallback.
 DL_HD float sin_f(float x) {
-    float s, c;
-    sincos_f(x, s, c);
-    return s;
+    if (isfinite(x) && x != 0.0f && fabsf(x) < 16.0f) {
+        float k = rintf(x * 0.6366197466850281f);
+        FF r = ff_two_sum(x - k * kPio2F1, -(k * kPio2F2));
+        r = ff_fast_sum(r.h, r.l - k * kPio2F3);
+        if (k == 0.0f || fabsf(r.h) > 1.52587890625e-05f) {
+            const int q = (int)k & 3;
+            FF r2 = ff_mul(r, r);
+            FF v = (q & 1) ? ff_cos_poly(r2) : ff_sin_poly(r, r2);
+            if (q & 2) v = ff_neg(v);
+            float s;
+            if (ff_rounds_to(v, s)) return s;
+        }
+    }
+    if (!isfinite(x)) return NAN;
+    double sd, cd;
+    sincos_d((double)x, sd, cd);
+    return (float)sd;
 }
 DL_HD float tan_f(float x) {
     if (!isfinite(x)) return NAN;

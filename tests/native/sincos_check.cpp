@@ -1,6 +1,6 @@
-// Compares the library's sin/cos and acos (binary32 double-float paths + rounding test, falling
-// back to binary64) with the binary64 paths alone over many arguments; prints mismatches and the
-// share of arguments that needed the binary64 path. Built and run by tests/test_math_paths.py.
+// Compares the library's sin/cos, sin alone and acos (binary32 double-float paths + rounding
+// test, falling back to binary64) with the binary64 paths alone over many arguments; prints
+// mismatches and the share of arguments that needed the binary64 path. Built and run by tests/test_math_paths.py.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -33,6 +33,11 @@ int main(int argc, char **argv) {
         float s64 = (float)sd, c64 = (float)cd;
         if (std::memcmp(&s, &s64, 4) || std::memcmp(&c, &c64, 4)) {
             if (mismatch < 10) std::printf("mismatch x=%a fast=(%a,%a) b64=(%a,%a)\n", x, s, c, s64, c64);
+            ++mismatch;
+        }
+        float s_only = dl::sin_f(x);  // the sin-only path
+        if (std::memcmp(&s_only, &s64, 4)) {
+            if (mismatch < 10) std::printf("sin mismatch x=%a fast=%a b64=%a\n", x, s_only, s64);
             ++mismatch;
         }
         // count fallbacks by re-running the fast path's reduction and test
