@@ -255,9 +255,8 @@ __device__ bool traverse(const DevScene &sc, f3 o, f3 dir, float max, bool alpha
             bool h0, h1;
             float n0, n1;
             box2(a, b, c, inv, oinv, ANY ? tmax : fminf(tmax, hit.t), h0, h1, n0, n1);
+            // an empty child (~0, only beside a root leaf) reads as a leaf of no triangles
             int r0 = __float_as_int(r.x), r1 = __float_as_int(r.y);
-            h0 = h0 && r0 != -1;  // ~0: an empty leaf
-            h1 = h1 && r1 != -1;
             if (h0 && h1) {
                 bool swap = n1 < n0;
                 stack[sp * stride] = swap ? r0 : r1;

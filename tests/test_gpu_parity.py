@@ -144,6 +144,24 @@ def test_empty_and_lightless_scenes():
     assert got.meshes[0].triangle_count() == 2
 
 
+@pytest.mark.parametrize("form", ["batched", "plain"])
+def test_two_triangle_scene_whose_bvh_root_is_a_leaf(form):
+    # one mesh of two triangles (a floor and a wall leaning over it): the occluder BVH is a single
+    # leaf beside an empty child; shadow, sky, soft sun and bounce rays all traverse it
+    pos = np.array([(-2, 0, -2), (2, 0, -2), (0, 0, 2), (-1.5, 0.2, 0.5), (1.5, 0.2, 0.5), (0, 2.5, -0.5)],
+                   np.float32)
+    uv = np.array([(0, 0), (0.45, 0), (0.2, 0.9), (0.55, 0.1), (1, 0.1), (0.8, 0.9)], np.float32)
+    mesh = dl.BakeMesh(id=1, positions=pos, indices=np.array([0, 2, 1, 3, 4, 5], np.uint32), uv1=uv)
+    bounce = dl.BakeBounce(samples=32)
+    lights = [fx.point_light(7, (0.3, 1.2, 1.5), 6.0), fx.sky_light(10),
+              fx.sun_light(9, (0.2, 1.0, 0.6), 0.53, illumination=dl.SINGLE_BOUNCE, bounce=bounce)]
+    inp, opts = dl.BakeInput([mesh], lights), fx.options(pixel_density=24.0, sky_samples=64, colored_bounce=True)
+    want, _, _ = oracle.bake(inp, opts)
+    got = dl.bake(inp, opts, form=form)
+    assert_same(got, want)
+    assert want.stats["rays"] > 0 and want.stats["bounce_rays"] > 0
+
+
 def test_errors_mirror_the_reference():
     inp, opts = fx.determinism_room()
     inp.meshes[1].id = 5
