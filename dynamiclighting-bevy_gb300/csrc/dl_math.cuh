@@ -532,14 +532,19 @@ DL_HD uint32_t rev_bits(uint32_t v) {
     return (v >> 16) | (v << 16);
 #endif
 }
+// The second coordinate of the (0, 2)-sequence (spread.rs:43-53): index bit k XORs in the
+// direction number v_k, v_0 = 2^31 and v_(k+1) = v_k ^ (v_k >> 1), so v_k has bit 31 - j set
+// exactly when j is a bit subset of k (Lucas). Bit 31 - j of the result is therefore the parity
+// of the index bits k that are supersets of j: a superset-parity transform over the 32 bit
+// positions (five shift-mask-xor steps) followed by a bit reversal, without a loop.
 DL_HD uint32_t sobol2(uint32_t index) {
-    uint32_t value = 0, dir = 1u << 31;
-    while (index != 0) {
-        if (index & 1u) value ^= dir;
-        index >>= 1;
-        dir ^= dir >> 1;
-    }
-    return value;
+    uint32_t x = index;
+    x ^= (x >> 1) & 0x55555555u;
+    x ^= (x >> 2) & 0x33333333u;
+    x ^= (x >> 4) & 0x0F0F0F0Fu;
+    x ^= (x >> 8) & 0x00FF00FFu;
+    x ^= (x >> 16) & 0x0000FFFFu;
+    return rev_bits(x);
 }
 DL_HD float unit24(uint32_t bits) { return (float)(bits >> 8) / 16777216.0f; }
 DL_HD f2 spread(uint32_t index, f2 off, bool rect) {

@@ -6,8 +6,19 @@
 
 #include "dl_host.hpp"
 
+// The reference's loop for the second coordinate (spread.rs:43-53), against the library's
+// closed form.
+static uint32_t sobol2_loop(uint32_t index) {
+    uint32_t value = 0, dir = 1u << 31;
+    for (; index != 0; index >>= 1, dir ^= dir >> 1)
+        if (index & 1u) value ^= dir;
+    return value;
+}
+
 int main() {
     int failures = 0;
+    for (uint64_t i = 0; i < (1ull << 32); i += i < (1u << 22) ? 1 : 4099)
+        failures += dl::sobol2((uint32_t)i) != sobol2_loop((uint32_t)i);
     for (uint32_t n : {16u, 64u, 256u, 1024u, 4096u}) {
         std::vector<uint16_t> order = dl::sky_sample_order(n);
         std::vector<int> seen(n, 0);
