@@ -220,9 +220,9 @@ __device__ __forceinline__ void box2(const float4 &a, const float4 &b, const flo
     n1 = en1;
 }
 
-// The reciprocal direction for the slab tests. It only prunes, so the fast reciprocal (about
-// 2 ulp) serves: its error scales an axis' slab distances by a common 1 + 2^-22, far inside the
-// boxes' padding (1e-5 of the coordinate scale) and the exit slack.
+// The reciprocal direction for the slab tests. It only prunes, so the fast reciprocal (within
+// 2 ulp) serves: each axis' slab distances all scale by one factor within 2^-22 of 1, so entry
+// and exit move by under 5e-7 of their value, inside box2's relative exit slack (2e-6).
 __device__ __forceinline__ f3 safe_inv(f3 d) {
     return f3{__fdividef(1.0f, d.x == 0.0f ? copysignf(1e-30f, d.x) : d.x),
               __fdividef(1.0f, d.y == 0.0f ? copysignf(1e-30f, d.y) : d.y),
