@@ -162,6 +162,20 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def whole_job(rays, ms, world, device):
+    """Replicas: each rank bakes its workload in `ms`; the job takes the slowest rank's time and
+    processes every rank's rays. Returns (rays/s of the job, the job's ms)."""
+    if world == 1:
+        return rays / (ms / 1e3), ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    n = torch.tensor([float(rays)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    return float(n.item()) / (float(t.item()) / 1e3), float(t.item())
+
+
 def flush_l2(torch_mod, buf):
     buf.zero_()
     torch_mod.cuda.synchronize()
@@ -217,13 +231,7 @@ def main():
     plain_result = plain.result()
     plain.close()
     rays = result.stats["rays"] + result.stats["bounce_rays"]
-    ms = statistics.median(dev_ms)
-    t_max = ms
-    if world > 1:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = rays * world / (t_max / 1e3)
+    value, t_max = whole_job(rays, statistics.median(dev_ms), world, f"cuda:{local}")
 
     # roofline of the dominant kernel (the persistent visibility kernel): algorithmic bytes from
     # an instrumented run of the same kernel on the same BVH (node visits x 64 B, triangle tests
@@ -265,7 +273,7 @@ def main():
             scene = dl.scene_from_c(out.contents)
         lib.dl_baked_scene_free(out)
     assert scene.words_equal(result) and scene.words_equal(plain_result), "forms disagree"
-    e2e_value = rays * world / (statistics.median(e2e_ms) / 1e3)
+    e2e_value, _ = whole_job(rays, statistics.median(e2e_ms), world, f"cuda:{local}")
 
     if rank != 0:
         return
