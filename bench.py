@@ -231,7 +231,8 @@ def main():
     plain_result = plain.result()
     plain.close()
     rays = result.stats["rays"] + result.stats["bounce_rays"]
-    value, t_max = whole_job(rays, statistics.median(dev_ms), world, f"cuda:{local}")
+    ms = statistics.median(dev_ms)
+    value, t_max = whole_job(rays, ms, world, f"cuda:{local}")
 
     # roofline of the dominant kernel (the persistent visibility kernel): algorithmic bytes from
     # an instrumented run of the same kernel on the same BVH (node visits x 64 B, triangle tests
