@@ -11,6 +11,7 @@
 #include <cstring>
 #include <future>
 #include <numeric>
+#include <atomic>
 #include <thread>
 
 namespace dl {
@@ -61,6 +62,26 @@ bool check_mesh(const dl_mesh &m, std::string &err) {
             return bad("alpha texture size doesn't match its data");
     }
     return true;
+}
+
+// Runs f(i) for i in [0, n) on the host's threads, taking indices from a shared counter (the
+// meshes of a scene differ in size by orders of magnitude). Small inputs run inline.
+template <class F>
+void for_each_index(uint32_t n, uint64_t work, F f) {
+    static const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    unsigned threads = work < 65536 ? 1u : std::min<unsigned>(hw, n);
+    if (threads <= 1) {
+        for (uint32_t i = 0; i < n; ++i) f(i);
+        return;
+    }
+    std::atomic<uint32_t> next{0};
+    auto body = [&] {
+        for (uint32_t i = next++; i < n; i = next++) f(i);
+    };
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < threads; ++t) pool.emplace_back(body);
+    body();
+    for (auto &th : pool) th.join();
 }
 
 bool unit_quat(const float q[4]) {
@@ -191,8 +212,19 @@ dl_status prepare_scene(const dl_bake_input &in, const dl_bake_options &o, HostS
             err = "two meshes share BakeId " + hex_id(s.meshes[i]->id);
             return DL_DUPLICATE_ID;
         }
-    for (auto *m : s.meshes)
-        if (!check_mesh(*m, err)) return DL_INVALID_MESH;
+    {
+        // every mesh checked on the host's threads; the first failure in sorted order reports
+        uint64_t work = 0;
+        for (auto *m : s.meshes) work += m->index_count + m->vertex_count;
+        std::vector<std::string> errs(s.meshes.size());
+        std::vector<uint8_t> ok(s.meshes.size(), 1);
+        for_each_index((uint32_t)s.meshes.size(), work, [&](uint32_t i) { ok[i] = check_mesh(*s.meshes[i], errs[i]); });
+        for (size_t i = 0; i < ok.size(); ++i)
+            if (!ok[i]) {
+                err = errs[i];
+                return DL_INVALID_MESH;
+            }
+    }
     std::vector<const dl_light *> lights;
     for (uint64_t i = 0; i < in.light_count; ++i) lights.push_back(&in.lights[i]);
     std::stable_sort(lights.begin(), lights.end(), [](auto *a, auto *b) { return a->id < b->id; });
@@ -302,12 +334,17 @@ dl_status prepare_scene(const dl_bake_input &in, const dl_bake_options &o, HostS
     }
 
     // PreparedMesh resolution (mesh_builder.rs:21-51, geometry.rs:66-70) and the occluders
-    // (occluder.rs:80-97)
-    for (uint32_t mi = 0; mi < s.meshes.size(); ++mi) {
+    // (occluder.rs:80-97): meshes on the host's threads, each mesh's area summed in triangle
+    // order and its occluders listed in triangle order, the lists joined in mesh order
+    const uint32_t M = (uint32_t)s.meshes.size();
+    std::vector<std::vector<uint32_t>> occ(M);
+    s.resolution.assign(M, 0);
+    uint64_t work = 0;
+    for (auto *m : s.meshes) work += m->index_count;
+    for_each_index(M, work, [&](uint32_t mi) {
         const dl_mesh &m = *s.meshes[mi];
         float area = 0.0f;
         uint64_t tris = m.index_count / 3;
-        s.triangles += tris;
         for (uint64_t t = 0; t < tris; ++t) {
             f3 v[3];
             for (int k = 0; k < 3; ++k) {
@@ -316,16 +353,25 @@ dl_status prepare_scene(const dl_bake_input &in, const dl_bake_options &o, HostS
             }
             f3 n = cross(sub(v[1], v[0]), sub(v[2], v[0]));
             area += length(n) * 0.5f;
-            if (m.occludes && length_sq(n) > 0.0f && std::isfinite(n.x) && std::isfinite(n.y) && std::isfinite(n.z)) {
-                s.occ_mesh.push_back(mi);
-                s.occ_tri.push_back((uint32_t)t);
-            }
+            if (m.occludes && length_sq(n) > 0.0f && std::isfinite(n.x) && std::isfinite(n.y) && std::isfinite(n.z))
+                occ[mi].push_back((uint32_t)t);
         }
         float size = ceilf(sqrtf(o.pixel_density * o.pixel_density * area));
         if (std::isnan(size)) size = 0.0f;
         uint32_t r = f2u(fminf(size, (float)o.max_lightmap_size));
         uint32_t hi = std::max(o.max_lightmap_size, 2u);
-        s.resolution.push_back(std::min(std::max(r, 2u), hi));
+        s.resolution[mi] = std::min(std::max(r, 2u), hi);
+    });
+    size_t total = 0;
+    for (uint32_t mi = 0; mi < M; ++mi) {
+        s.triangles += s.meshes[mi]->index_count / 3;
+        total += occ[mi].size();
+    }
+    s.occ_mesh.reserve(total);
+    s.occ_tri.reserve(total);
+    for (uint32_t mi = 0; mi < M; ++mi) {
+        s.occ_mesh.insert(s.occ_mesh.end(), occ[mi].size(), mi);
+        s.occ_tri.insert(s.occ_tri.end(), occ[mi].begin(), occ[mi].end());
     }
     return DL_OK;
 }
