@@ -2673,6 +2673,16 @@ struct HostResult {
     dl_sky_probes probes{};
 };
 
+// Copies n words into host memory mapped for the device (pinned, written over the CPU-GPU link
+// by the SMs): 16-byte stores, the tail word by word.
+__global__ void k_copy_words(const uint32_t *src, uint32_t *dst, uint64_t n) {
+    const uint64_t n4 = n / 4, stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+    uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) d4[i] = s4[i];
+    for (uint64_t i = n4 * 4 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) dst[i] = src[i];
+}
+
 // The last run's scene. With `download` false the triangle words, distance cubes and sun map
 // texels stay on the device and the scene's pointers to them are device pointers (for the
 // device-side payload encode); everything else is on the host either way.
@@ -2687,7 +2697,18 @@ dl_status assemble(dl_session &s, std::unique_ptr<HostResult> &r, bool download)
     if (download) {
         r->buffer = word_cache().take(s.out_words);
         r->words = r->buffer.p;
-        if (s.out_words) CK(cudaMemcpy(r->words, s.words_dev, s.out_words * 4, cudaMemcpyDeviceToHost));
+        uint32_t *mapped = nullptr;
+        if (s.out_words && r->buffer.pinned &&
+            cudaHostGetDevicePointer((void **)&mapped, r->words, 0) == cudaSuccess) {
+            // the SMs write the words into the pinned buffer: as fast as the copy engine here,
+            // and steadier (the copy engine's rate varied 10x between sessions on some machines)
+            k_copy_words<<<s.sms * 8, 256, 0, s.stream>>>(s.words_dev, mapped, s.out_words);
+            LAUNCHED("k_copy_words");
+            CK(cudaStreamSynchronize(s.stream));
+        } else if (s.out_words) {
+            cudaGetLastError();  // a buffer the device cannot map: the copy engine
+            CK(cudaMemcpy(r->words, s.words_dev, s.out_words * 4, cudaMemcpyDeviceToHost));
+        }
         words = r->words;
         s.report.d2h_bytes = s.out_words * 4 + (s.mesh_words.size() * 8) + sizeof(Counters);
     }
