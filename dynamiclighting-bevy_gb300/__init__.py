@@ -414,6 +414,8 @@ def load_library(path: str = LIBRARY_PATH):
     lib.dl_free.argtypes = [C.c_void_p]
     lib.dl_session_encode_payload.restype = C.c_int
     lib.dl_session_encode_payload.argtypes = [C.c_void_p, P(P(C.c_uint8)), P(C.c_uint64), P(C.c_uint32)]
+    lib.dl_release_memory.restype = None
+    lib.dl_release_memory.argtypes = []
     lib.dl_session_occluder_bvh.restype = C.c_int
     lib.dl_session_occluder_bvh.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64,
                                             P(C.c_uint32), P(C.c_uint32)]

@@ -1451,11 +1451,31 @@ struct CudaError {
         if (e__ != cudaSuccess) throw CudaError{e__, name};  \
     } while (0)
 
-template <class T>
-T *dev_alloc(std::vector<void *> &owned, size_t count, uint64_t &bytes) {
+// Device memory comes from the device's default stream-ordered pool, allocated and freed on the
+// session's stream. The pool keeps what sessions free (its release threshold is raised once per
+// device), so the next bake's allocations reuse it without new cudaMalloc/cudaFree calls;
+// dl_release_memory hands it back to the driver.
+void keep_freed_device_memory(int device) {
+    static std::mutex lock;
+    static std::vector<int> done;
+    std::lock_guard<std::mutex> guard(lock);
+    if (std::find(done.begin(), done.end(), device) != done.end()) return;
+    cudaMemPool_t pool;
+    CK(cudaDeviceGetDefaultMemPool(&pool, device));
+    uint64_t keep = ~0ull;
+    CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    done.push_back(device);
+}
+void *dev_malloc(size_t bytes, cudaStream_t st) {
     void *p = nullptr;
+    CK(cudaMallocAsync(&p, std::max<size_t>(bytes, 16), st));
+    return p;
+}
+
+template <class T>
+T *dev_alloc(std::vector<void *> &owned, cudaStream_t st, size_t count, uint64_t &bytes) {
     size_t b = std::max<size_t>(count * sizeof(T), 16);
-    CK(cudaMalloc(&p, b));
+    void *p = dev_malloc(b, st);
     owned.push_back(p);
     bytes += b;
     return static_cast<T *>(p);
@@ -1467,9 +1487,11 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 
 }  // namespace
 
-// A named pool of device buffers, grown on demand and reused across runs of one session.
+// A named pool of device buffers, grown on demand and reused across runs of one session;
+// allocated and freed on the session's stream.
 struct Pool {
     std::map<std::string, std::pair<void *, size_t>> bufs;
+    cudaStream_t stream = nullptr;
     uint64_t bytes = 0;
     uint64_t generation = 0;  // bumped whenever a buffer moves
     template <class T>
@@ -1478,18 +1500,19 @@ struct Pool {
         auto it = bufs.find(name);
         if (it != bufs.end() && it->second.second >= b) return static_cast<T *>(it->second.first);
         if (it != bufs.end()) {
-            cudaFree(it->second.first);
+            cudaFreeAsync(it->second.first, stream);
             bytes -= it->second.second;
         }
-        void *p = nullptr;
-        CK(cudaMalloc(&p, b));
+        void *p = dev_malloc(b, stream);
         bufs[name] = {p, b};
         bytes += b;
         ++generation;
         return static_cast<T *>(p);
     }
-    ~Pool() {
-        for (auto &kv : bufs) cudaFree(kv.second.first);
+    // Frees every buffer on the stream; the session calls it before destroying its stream.
+    void release() {
+        for (auto &kv : bufs) cudaFreeAsync(kv.second.first, stream);
+        bufs.clear();
     }
 };
 
@@ -1546,8 +1569,13 @@ struct dl_session {
         if (graph) cudaGraphExecDestroy(graph);
         for (auto &e : marks)
             if (e) cudaEventDestroy(e);
-        for (void *p : owned) cudaFree(p);
-        if (stream) cudaStreamDestroy(stream);
+        if (stream) {
+            // back to the stream-ordered pool (kept for the next session), in stream order
+            pool.release();
+            for (void *p : owned) cudaFreeAsync(p, stream);
+            cudaStreamSynchronize(stream);
+            cudaStreamDestroy(stream);
+        }
         if (side) cudaStreamDestroy(side);
     }
 };
@@ -1646,6 +1674,8 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     CK(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device));
     CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+    keep_freed_device_memory(s->device);
+    s->pool.stream = s->stream;
 
     // flatten meshes
     uint32_t M = (uint32_t)h.meshes.size();
@@ -1701,8 +1731,8 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     uint64_t &bytes = s->scene_bytes;
     auto up = [&](const void *src, size_t n, auto *&dst) {
         using T = std::remove_const_t<std::remove_pointer_t<std::remove_reference_t<decltype(dst)>>>;
-        T *p = dev_alloc<T>(s->owned, n / sizeof(T) + 1, bytes);
-        if (n) CK(cudaMemcpy(p, src, n, cudaMemcpyHostToDevice));
+        T *p = dev_alloc<T>(s->owned, s->stream, n / sizeof(T) + 1, bytes);
+        if (n) CK(cudaMemcpyAsync(p, src, n, cudaMemcpyHostToDevice, s->stream));
         dst = p;
         s->report.h2d_bytes += n;
     };
@@ -1744,7 +1774,7 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
                           sc.occ_tri, N};
         DeviceBvh db;
         try {
-            build_bvh_device(bi, [&](size_t b) { return (void *)dev_alloc<uint8_t>(s->owned, b, bytes); }, s->stream,
+            build_bvh_device(bi, [&](size_t b) { return (void *)dev_alloc<uint8_t>(s->owned, s->stream, b, bytes); }, s->stream,
                              db);
         } catch (const DeviceBvhError &e) {
             throw CudaError{e.code, e.what};
@@ -1764,11 +1794,11 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
         sc.tri_e2 = db.tri_e2;
         sc.occ_leaf = db.occ_leaf;
         if (N == 0) {  // no occluders: small placeholders, which traversal never reads
-            sc.nodes = dev_alloc<float4>(s->owned, 4, bytes);
-            sc.tri_v0 = dev_alloc<float4>(s->owned, 1, bytes);
-            sc.tri_e1 = dev_alloc<float4>(s->owned, 1, bytes);
-            sc.tri_e2 = dev_alloc<float4>(s->owned, 1, bytes);
-            sc.occ_leaf = dev_alloc<uint32_t>(s->owned, 1, bytes);
+            sc.nodes = dev_alloc<float4>(s->owned, s->stream, 4, bytes);
+            sc.tri_v0 = dev_alloc<float4>(s->owned, s->stream, 1, bytes);
+            sc.tri_e1 = dev_alloc<float4>(s->owned, s->stream, 1, bytes);
+            sc.tri_e2 = dev_alloc<float4>(s->owned, s->stream, 1, bytes);
+            sc.occ_leaf = dev_alloc<uint32_t>(s->owned, s->stream, 1, bytes);
         }
     }
     sc.triangles = T;
@@ -1801,8 +1831,10 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     sc.colored_bounce = o->colored_bounce;
     sc.refine_eps = s->config.refine_epsilon;
     sc.refine_eps2 = sc.refine_eps * sc.refine_eps;
-    s->ctr = dev_alloc<Counters>(s->owned, 1, bytes);
-    s->cancel_dev = dev_alloc<uint32_t>(s->owned, 1, bytes);
+    s->ctr = dev_alloc<Counters>(s->owned, s->stream, 1, bytes);
+    s->cancel_dev = dev_alloc<uint32_t>(s->owned, s->stream, 1, bytes);
+    CK(cudaStreamSynchronize(s->stream));  // allocations and uploads done (the side stream and
+                                           // synchronous copies use them from here on)
     for (auto &e : s->marks) CK(cudaEventCreate(&e));
     s->report.ms_host[2] = ms_since(t_up) - ms_bvh_device;
     s->report.bvh_nodes = h.bvh_node_count;
@@ -2635,6 +2667,12 @@ struct WordCache {
         cudaGetLastError();  // no pinned memory to be had: a pageable buffer (a slower copy)
         return Buffer{cap, new uint32_t[cap], false};
     }
+    void clear() {
+        std::lock_guard<std::mutex> guard(lock);
+        for (const Buffer &b : free) release(b);
+        free.clear();
+        held = 0;
+    }
     void give(const Buffer &b) {
         std::lock_guard<std::mutex> guard(lock);
         while (held + b.cap * 4 > kCacheBytes && !free.empty()) {  // drop the oldest
@@ -3148,6 +3186,16 @@ dl_status dl_session_report(const dl_session *s, dl_bake_report *report) {
 }
 
 void dl_session_destroy(dl_session *s) { delete s; }
+
+void dl_release_memory(void) {
+    word_cache().clear();
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return;
+    for (int d = 0; d < n; ++d) {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, d) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
+    }
+}
 
 void dl_baked_scene_free(dl_baked_scene *scene) { delete reinterpret_cast<HostResult *>(scene); }
 

@@ -687,18 +687,19 @@ __global__ void k_leaf_triangles(DeviceBvhInput in, const uint32_t *idx, DeviceB
 
 uint32_t blocks_for(uint64_t n, uint32_t threads) { return (uint32_t)std::max<uint64_t>(1, (n + threads - 1) / threads); }
 
-// Scratch device memory freed when the build ends.
+// Scratch device memory from the stream-ordered pool, freed on the build's stream when it ends.
 struct Scratch {
+    cudaStream_t stream;
     std::vector<void *> held;
     template <class T>
     T *get(size_t n) {
         void *p = nullptr;
-        BK(cudaMalloc(&p, std::max<size_t>(n * sizeof(T), 16)));
+        BK(cudaMallocAsync(&p, std::max<size_t>(n * sizeof(T), 16), stream));
         held.push_back(p);
         return static_cast<T *>(p);
     }
     ~Scratch() {
-        for (void *p : held) cudaFree(p);
+        for (void *p : held) cudaFreeAsync(p, stream);
     }
 };
 
@@ -709,7 +710,7 @@ void build_bvh_device(const DeviceBvhInput &in, const std::function<void *(size_
     const uint32_t n = in.occluders;
     out = DeviceBvh{};
     if (n == 0) return;
-    Scratch sc;
+    Scratch sc{stream, {}};
     State st;
     st.plo = sc.get<float4>(n);
     st.phi = sc.get<float4>(n);
@@ -826,7 +827,10 @@ void build_bvh_device(const DeviceBvhInput &in, const std::function<void *(size_
     BK(cudaMemcpyAsync(&root, st.nodes, sizeof root, cudaMemcpyDeviceToHost, stream));
     uint32_t inner = 1;
     BK(cudaStreamSynchronize(stream));
-    if (root.inner) BK(cudaMemcpy(&inner, L.size, 4, cudaMemcpyDeviceToHost));
+    if (root.inner) {
+        BK(cudaMemcpyAsync(&inner, L.size, 4, cudaMemcpyDeviceToHost, stream));
+        BK(cudaStreamSynchronize(stream));
+    }
     out.node_count = inner;
     out.nodes = static_cast<BvhNode *>(alloc((size_t)inner * sizeof(BvhNode)));
     out.tri_v0 = static_cast<float4 *>(alloc((size_t)n * sizeof(float4)));

@@ -362,6 +362,10 @@ dl_status dl_session_occluder_bvh(dl_session *session, void *nodes, uint64_t nod
 dl_status dl_session_bounce_map(dl_session *session, uint64_t mesh_id, uint32_t slot, uint32_t rect[4],
                                 float *rgb, uint32_t cap, uint32_t *texels);
 void dl_session_destroy(dl_session *session);
+/* No counterpart in the reference: device memory that finished sessions freed stays in the
+   device's stream-ordered pool, and downloaded results' pinned host buffers stay cached, for the
+   next bake; this hands both back (to the driver and the host). Call it between bakes. */
+void dl_release_memory(void);
 
 /* ---- .dynlight payload (src/bake/format/mod.rs:101-213): the uncompressed payload bytes and
  * its CRC-32 (IEEE). The file's gzip layer is left to the caller's deflate library. */

@@ -205,6 +205,18 @@ def test_sessions_repeat_identically():
     assert a.words_equal(b) and a.stats == b.stats
 
 
+def test_bakes_after_releasing_the_cached_memory_repeat():
+    # device memory that sessions free stays pooled for the next bake; dl_release_memory hands
+    # it back, and the next bake allocates afresh
+    inp, opts = fx.determinism_room()
+    first = dl.bake(inp, opts)
+    again = dl.bake(inp, opts)
+    dl.load_library().dl_release_memory()
+    fresh = dl.bake(inp, opts)
+    assert_same(again, first)
+    assert_same(fresh, first)
+
+
 def test_tuning_does_not_change_the_bytes():
     # the GPU analogue of the reference's 1/4/7-thread determinism (determinism.rs:65-72)
     inp, opts = scenes.soft_rooms(rooms=2, lights=16, boxes_per_room=4)
