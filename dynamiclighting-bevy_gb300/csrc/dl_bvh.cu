@@ -362,9 +362,9 @@ __global__ void __launch_bounds__(kThreads) k_level_scatter(State st, Level lv) 
         unsigned bl = __ballot_sync(0xFFFFFFFFu, left), bv = __ballot_sync(0xFFFFFFFFu, valid);
         if (lane == 0) wl[warp] = __popc(bl);
         __syncthreads();
-        uint32_t before_l = 0, before_v = 0;
+        uint32_t before_l = 0;
         for (uint32_t w = 0; w < warp; ++w) before_l += wl[w];
-        before_v = warp * 32;  // every earlier warp's items are valid when this one has any
+        const uint32_t before_v = warp * 32;  // every earlier warp's items are valid when this one has any
         unsigned below = (1u << lane) - 1u;
         uint32_t rank_l = before_l + __popc(bl & below);
         uint32_t rank_r = (before_v - before_l) + __popc(bv & ~bl & below);
