@@ -1,9 +1,9 @@
-"""The bake at the full sizes of the benchmark configurations, through properties that do not
-depend on size: the batched and plain forms agree word for word (two different schedules of the
-same per-texel work), launch shapes and sample orders change no byte, a session repeats
-identically, the occluder BVH built on the device and on the host gives the same bytes, and the
-payload encoded next to the resident words equals the host encoding with zlib's CRC-32. The
-oracle checks the same kernels on the smaller cases of the other GPU tests."""
+"""The bake at the full sizes of the benchmark configurations: the outdoor scene against the
+oracle word for word, and properties that do not depend on size — the batched and plain forms
+agree word for word (two different schedules of the same per-texel work), launch shapes and
+sample orders change no byte, a session repeats identically, the occluder BVH built on the
+device and on the host gives the same bytes, and the payload encoded next to the resident words
+equals the host encoding with zlib's CRC-32."""
 import zlib
 
 import pytest
@@ -19,6 +19,16 @@ pytestmark = pytest.mark.gpu
 @pytest.fixture(scope="module")
 def outdoor():
     return scenes.outdoor()  # C4: 546k triangles, sun + sky + 32 points, colored sun bounce
+
+
+def test_outdoor_matches_the_oracle_at_full_size(outdoor):
+    # the oracle on every host core (about 90 s on 16 cores): every word and statistic
+    import os
+    from oracle import oracle
+    inp, opts = outdoor
+    got = dl.bake(inp, opts)
+    want, _, _ = oracle.bake(inp, opts, threads=os.cpu_count() or 1)
+    assert_same(got, want)
 
 
 def test_outdoor_forms_and_launch_shapes_agree(outdoor):
