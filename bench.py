@@ -310,7 +310,7 @@ def main():
                      "node_visits": int(crep.node_visits), "tri_tests": int(crep.tri_tests),
                      "items": int(crep.work_items)},
     }
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and world == 1:  # the CPU baseline: rank 0 of a 1-GPU run
         cb = cpu_baseline(args.workload)
         cb.pop("seconds")
         line["cpu_baseline"] = cb
