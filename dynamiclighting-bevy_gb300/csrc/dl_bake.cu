@@ -1455,16 +1455,24 @@ struct CudaError {
 // session's stream. The pool keeps what sessions free (its release threshold is raised once per
 // device), so the next bake's allocations reuse it without new cudaMalloc/cudaFree calls;
 // dl_release_memory hands it back to the driver.
+std::mutex g_pool_lock;
+std::vector<int> g_pooled_devices;  // devices whose default pool keeps freed memory
 void keep_freed_device_memory(int device) {
-    static std::mutex lock;
-    static std::vector<int> done;
-    std::lock_guard<std::mutex> guard(lock);
-    if (std::find(done.begin(), done.end(), device) != done.end()) return;
+    std::lock_guard<std::mutex> guard(g_pool_lock);
+    if (std::find(g_pooled_devices.begin(), g_pooled_devices.end(), device) != g_pooled_devices.end()) return;
     cudaMemPool_t pool;
     CK(cudaDeviceGetDefaultMemPool(&pool, device));
     uint64_t keep = ~0ull;
     CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
-    done.push_back(device);
+    g_pooled_devices.push_back(device);
+}
+// Returns the pooled memory of every device the library has baked on (no other device is touched).
+void release_pooled_device_memory() {
+    std::lock_guard<std::mutex> guard(g_pool_lock);
+    for (int d : g_pooled_devices) {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, d) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
+    }
 }
 void *dev_malloc(size_t bytes, cudaStream_t st) {
     void *p = nullptr;
@@ -3189,12 +3197,7 @@ void dl_session_destroy(dl_session *s) { delete s; }
 
 void dl_release_memory(void) {
     word_cache().clear();
-    int n = 0;
-    if (cudaGetDeviceCount(&n) != cudaSuccess) return;
-    for (int d = 0; d < n; ++d) {
-        cudaMemPool_t pool;
-        if (cudaDeviceGetDefaultMemPool(&pool, d) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
-    }
+    release_pooled_device_memory();
 }
 
 void dl_baked_scene_free(dl_baked_scene *scene) { delete reinterpret_cast<HostResult *>(scene); }
