@@ -53,10 +53,6 @@ struct DevScene {
     const uint16_t *order_cells, *cell_samples;
 };
 constexpr uint32_t kMaxOrdered = 4096;
-// The coherent order of n samples, or null when n is not a power of two from 16 to kMaxOrdered.
-__device__ __forceinline__ const uint16_t *sample_order(const DevScene &sc, uint32_t n) {
-    return (n >= 16 && n <= kMaxOrdered && !(n & (n - 1))) ? sc.orders + (n - 16) : nullptr;
-}
 // The shift of a net of n samples (n a power of two from 16 to kMaxOrdered) by `off` in whole
 // cells, packed as x | y << 8 | xbits << 16 | ybits << 24.
 __device__ __forceinline__ uint32_t net_shift(uint32_t n, f2 off) {
