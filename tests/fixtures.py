@@ -81,3 +81,32 @@ def determinism_room():
               sun_light(25, (0.3, 1.0, 0.2), 0.53), sun_light(15, (-0.5, 1.0, 0.4), 0.0),
               sky_light(12)]
     return dl.BakeInput(meshes, lights), options(pixel_density=12.0, sky_samples=16)
+
+
+def triangle_texels(mesh, triangle, size, face=None):
+    """The texels whose centers triangle `triangle` of `mesh` covers in a `size`-texel map
+    (src/bake/texels.rs triangle_texels, through the oracle), as [(x, y, position)]. `face`
+    defaults to the normalized cross product of the triangle's edges."""
+    import ctypes as C
+    from oracle import oracle as orc
+    corners = [int(c) for c in mesh.indices[3 * triangle: 3 * triangle + 3]]
+    v = np.float32([mesh.positions[c] for c in corners])
+    n = (np.float32([mesh.normals[c] for c in corners]) if mesh.normals is not None
+         else np.tile(np.float32([0, 1, 0]), (3, 1)))
+    uv = np.float32([mesh.uv1[c] for c in corners])
+    if face is None:
+        c = np.cross(v[1] - v[0], v[2] - v[0]).astype(np.float32)
+        face = c / np.float32(np.linalg.norm(c))
+    face = np.ascontiguousarray(face, np.float32)
+    cap = size * size
+    xy = np.zeros(2 * cap, np.uint32)
+    pos = np.zeros(3 * cap, np.float32)
+    nrm = np.zeros(3 * cap, np.float32)
+    args = [np.ascontiguousarray(a.reshape(-1)) for a in (v, n, uv)]
+    count = orc.lib().oracle_texels(0, *(a.ctypes.data_as(C.c_void_p) for a in args),
+                                    face.ctypes.data_as(C.c_void_p), size, None, cap,
+                                    xy.ctypes.data_as(C.c_void_p), pos.ctypes.data_as(C.c_void_p),
+                                    nrm.ctypes.data_as(C.c_void_p))
+    assert count <= cap
+    xy, pos = xy[:2 * count].reshape(-1, 2), pos[:3 * count].reshape(-1, 3)
+    return [(int(a), int(b), p) for (a, b), p in zip(xy, pos)]
