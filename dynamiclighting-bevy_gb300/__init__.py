@@ -572,3 +572,7 @@ def encode_payload(scene_c) -> tuple:
         return bytes(np.ctypeslib.as_array(data, shape=(length.value,))), crc.value
     finally:
         lib.dl_free(data)
+
+
+# The .dynlight file and the shader-side word reader: host code over finished bakes.
+from . import dynlight_file, mirror  # noqa: E402,F401
