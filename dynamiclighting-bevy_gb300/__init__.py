@@ -170,7 +170,10 @@ class BakeProgress:
         return self.raw.stage
 
     def fraction(self):
-        return self.raw.done / self.raw.total if self.raw.total else 0.0
+        """Progress through the current stage, 0 to 1; 1 once the bake is done (progress.rs:71-81)."""
+        if self.raw.stage >= 4:  # BakeStage::Done, or a stage past the known ones
+            return 1.0
+        return min(self.raw.done / self.raw.total, 1.0) if self.raw.total else 0.0
 
 
 # ---- marshalling ----------------------------------------------------------------------------

@@ -2631,9 +2631,10 @@ dl_status run(dl_session &s, dl_progress *progress) {
     s.bounce_map = bmap;
     s.region_rect = region_rect;
     s.have_result = true;
-    if (progress) {
-        progress->done = M;
-        progress->stage = 4;  // Done
+    if (progress) {  // BakeStage::Done with its counters cleared, as progress.begin(Done, 0) leaves them
+        progress->done = 0;
+        progress->total = 0;
+        progress->stage = 4;
     }
     return DL_OK;
 }

@@ -732,9 +732,23 @@ struct Result {
     uint64_t burial_rays = 0, photon_rays = 0;
 };
 
+// BakeProgress::begin and advance (src/bake/progress.rs:91-100) on the caller's counters, which
+// the bake writes and the caller reads from another thread.
+static void progress_begin(const dl_progress *p, uint32_t stage, uint64_t total) {
+    if (!p) return;
+    auto *w = const_cast<dl_progress *>(p);
+    w->done = 0;
+    w->total = total;
+    w->stage = stage;
+}
+static void progress_advance(const dl_progress *p, uint64_t items) {
+    if (p) const_cast<dl_progress *>(p)->done = p->done + items;
+}
+
 static bool bake(const dl_bake_input &in, const dl_bake_options &o, const dl_progress *progress, bool brute,
                  Result &res, Error &err) {
     if (!validate_options(o, err)) return false;
+    progress_begin(progress, 0, 0);  // BakeStage::Preparing (baker.rs:33)
     // sorted_meshes / sorted_lights (baker.rs:205-233)
     std::vector<const dl_mesh *> meshes;
     for (uint64_t i = 0; i < in.mesh_count; ++i) meshes.push_back(&in.meshes[i]);
@@ -796,6 +810,9 @@ static bool bake(const dl_bake_input &in, const dl_bake_options &o, const dl_pro
             sc.tan_radius[s] = tan_f(l.sun_angular_radius());
         }
     }
+    uint64_t bounce_lights = 0;
+    for (auto &l : sc.lights) bounce_lights += l.bakes_bounce(o) ? 1 : 0;
+    progress_begin(progress, 1, bounce_lights);  // BakeStage::PhotonCubes (baker.rs:56-57)
     for (size_t s = 0; s < L; ++s) {
         const Light &l = sc.lights[s];
         if (!l.bakes_bounce(o) || sc.cancelled()) continue;
@@ -806,6 +823,7 @@ static bool bake(const dl_bake_input &in, const dl_bake_options &o, const dl_pro
             sc.cubes[s] = build_photon_cube(l, sc.occluders, o.photon_cube_resolution);
             res.photon_rays += (uint64_t)6 * o.photon_cube_resolution * o.photon_cube_resolution;
         }
+        progress_advance(progress, 1);
     }
     if (sc.cancelled()) {
         err = Error{DL_CANCELLED, "the bake was cancelled"};
@@ -814,8 +832,10 @@ static bool bake(const dl_bake_input &in, const dl_bake_options &o, const dl_pro
     std::vector<Prepared> prepared;
     for (auto *m : meshes) prepared.push_back(prepare(m, o));
     std::vector<MeshOut> outs;
+    progress_begin(progress, 2, prepared.size());  // BakeStage::Meshes (baker.rs:84-89)
     for (auto &p : prepared) {
         outs.push_back(bake_mesh(sc, p));
+        progress_advance(progress, 1);
         if (sc.cancelled()) {
             err = Error{DL_CANCELLED, "the bake was cancelled"};
             return false;
@@ -853,6 +873,16 @@ static bool bake(const dl_bake_input &in, const dl_bake_options &o, const dl_pro
     }
     res.bvh = sc.light_bvh.nodes;
     // distance cubes, sun maps, sky probes (baker.rs:114-152)
+    {
+        const bool maps = o.dynamic_geometry != DL_GEOMETRY_LIGHTING_ONLY;
+        uint64_t n_suns = 0, n_skies = 0;
+        for (size_t s = sc.local_lights; s < sc.lights.size(); ++s) {
+            n_suns += sc.lights[s].l->shape == DL_SHAPE_SUN ? 1 : 0;
+            n_skies += sc.lights[s].l->shape == DL_SHAPE_SKY ? 1 : 0;
+        }
+        // BakeStage::DistanceCubes (baker.rs:117-120)
+        progress_begin(progress, 3, (uint64_t)sc.local_lights * 6 + (maps ? n_suns : 0) + (maps && n_skies ? 1 : 0));
+    }
     if (o.dynamic_geometry != DL_GEOMETRY_LIGHTING_ONLY) {
         res.distance_cubes = bake_distance_cubes(sc.lights, sc.local_lights, sc.occluders);
         bool any_sky = false, sky_alpha = false;
@@ -918,6 +948,7 @@ static bool bake(const dl_bake_input &in, const dl_bake_options &o, const dl_pro
     s.sun_maps = res.sun_maps.data();
     s.sky_probes = res.probes.present ? &res.sky_probes : nullptr;
     s.stats = stats;
+    progress_begin(progress, 4, 0);  // BakeStage::Done (baker.rs:201)
     return true;
 }
 

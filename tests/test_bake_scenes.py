@@ -4,7 +4,8 @@ reference's own thresholds: analytic shadow footprints under point lights
 probes (sky.rs), meshes that cast no shadow and decals (shadowless.rs), texels inside boxes, thin
 strips and buried islands (coverage.rs), local bounce (bounce.rs), sun and colored bounce
 (colored_bounce.rs), determinism and output order (determinism.rs), the word layout (layout.rs),
-and area light penumbrae against brute force (tests/area_light_bake.rs, without its ECS app).
+area light penumbrae against brute force (tests/area_light_bake.rs, without its ECS app), and
+the public bake API's file round trip and shader-side reads (tests/bake_api.rs).
 
 Every test runs on two bakers: the oracle on the CPU, and the CUDA library's batched form under
 the gpu marker. Passing on the oracle pins the restatement to the reference's analytic answers;
@@ -29,8 +30,8 @@ Y = np.float32([0, 1, 0])
 def baker(request):
     """bake(inp, opts) on the oracle (CPU) or through the CUDA library."""
     if request.param == "oracle":
-        return lambda inp, opts: oracle.bake(inp, opts)[0]
-    return lambda inp, opts: dl.bake(inp, opts)
+        return lambda inp, opts, progress=None: oracle.bake(inp, opts, progress=progress)[0]
+    return lambda inp, opts, progress=None: dl.bake(inp, opts, progress)
 
 
 def mesh_of(baked, mesh_id):
@@ -691,3 +692,56 @@ def test_point_lights_keep_one_shadow_bit(baker):
     assert baked.stats["rays"] > 0 and baked.stats["texels"] > 0
     values = floor_shadows(baked)[1]
     assert np.all((values == 0.0) | (values == 1.0)) and np.any(values == 0.0), "the box casts a shadow"
+
+
+# ---- tests/bake_api.rs: bake, write and read the file, read the result like the runtime -------
+
+def api_input():
+    floor = dl.BakeMesh(id=7, positions=np.float32([[-2, 0, -2], [2, 0, -2], [2, 0, 2], [-2, 0, 2]]),
+                        indices=np.uint32([0, 2, 1, 0, 3, 2]), uv1=np.float32([[0, 0], [1, 0], [1, 1], [0, 1]]),
+                        normals=np.tile(Y, (4, 1)))
+    return dl.BakeInput([floor], [fx.point_light(2, (1.0, 1.0, 0.0), 3.0), fx.point_light(1, (-1.0, 1.0, 0.0), 3.0)])
+
+
+def test_bake_encode_decode_round_trip(baker):
+    from dynlight_gb300 import dynlight_file as f
+    progress = dl.BakeProgress()
+    scene = baker(api_input(), dl.BakeOptions(pixel_density=4.0, dynamic_geometry=dl.ANGULAR), progress)
+    assert progress.stage == 4 and progress.fraction() == 1.0  # BakeStage::Done
+    data = f.encode(scene)
+    assert data[:8] == b"DYNLIGHT" and data[8:12] == (6).to_bytes(4, "little")
+    back = f.decode(data)
+    assert digest(back) == digest(scene)
+    assert f.encode(back) == data, "encoding is canonical"
+    future = bytearray(data)
+    future[8:12] = (7).to_bytes(4, "little")
+    with pytest.raises(f.FormatError) as e:
+        f.decode(bytes(future))
+    assert e.value == f.FormatError("UnsupportedVersion", found=7) and "re-bake" in str(e.value)
+
+
+def cube_index(direction, res=64):
+    """texel_index(direction_to_texel(d)) (src/shared/cube.rs:94-96) through the oracle."""
+    out = np.zeros(3, np.uint32)
+    oracle.lib().oracle_cube_texel(oracle.ptr(np.float32(direction)), res, oracle.ptr(out))
+    face, x, y = (int(v) for v in out)
+    return face * res * res + y * res + x
+
+
+def test_baked_scene_reads_like_the_shader(baker):
+    from dynlight_gb300.mirror import DISTANCE_CUBE_WORDS, distance_cube_value
+    scene = baker(api_input(), dl.BakeOptions(pixel_density=4.0, dynamic_geometry=dl.ANGULAR))
+    assert scene.light_bvh.shape == (1, 8) and scene.light_bvh[0][7] == 2, "two lights fit one leaf"
+    mesh = scene.meshes[0]
+    assert mesh.resolution == 16 and mesh.triangle_count() == 2
+    for t in range(2):  # both lights reach both triangles, entries in BVH slot order
+        v = TriangleView.load(mesh.triangles, t, False)
+        assert v.light_count == 2
+        for k in range(2):
+            assert v.light(k).light_index == k
+            assert v.shadow_bit(v.light(k), 8, 8) is True, "nothing blocks the floor"
+    # angular distance cubes: exact distances, the floor 1 m below each light; misses store the radius
+    assert scene.distance_cubes.size == 2 * DISTANCE_CUBE_WORDS
+    for slot in range(2):
+        assert abs(distance_cube_value(scene.distance_cubes, slot, cube_index((0, -1, 0))) - 1.0) < 0.01
+        assert distance_cube_value(scene.distance_cubes, slot, cube_index((0, 1, 0))) == 3.0
