@@ -1342,4 +1342,59 @@ void oracle_slerp(const float a[3], const float b[3], float s, float out[3]) {
     out[0] = r.x; out[1] = r.y; out[2] = r.z;
 }
 
+// ---- geometry.rs helpers (geometry.rs:19-140) ----
+static V3 v3_at(const float *p) { return V3{p[0], p[1], p[2]}; }
+void oracle_closest_point(const float p[3], const float tri[9], float out[3]) {
+    V3 r = closest_point_on_triangle(v3_at(p), v3_at(tri), v3_at(tri + 3), v3_at(tri + 6));
+    out[0] = r.x; out[1] = r.y; out[2] = r.z;
+}
+int oracle_sphere_triangle(const float center[3], float radius, const float tri[9]) {
+    return sphere_intersects_triangle(v3_at(center), radius, v3_at(tri), v3_at(tri + 3), v3_at(tri + 6)) ? 1 : 0;
+}
+// 1 and the weights when `p` lies in the UV triangle `t` (either winding), else 0.
+int oracle_uv_barycentrics(const float t[6], const float p[2], float out[3]) {
+    V2 tt[3] = {V2{t[0], t[1]}, V2{t[2], t[3]}, V2{t[4], t[5]}};
+    V3 w{0, 0, 0};
+    bool inside = uv_barycentrics(tt, V2{p[0], p[1]}, w);
+    out[0] = w.x; out[1] = w.y; out[2] = w.z;
+    return inside ? 1 : 0;
+}
+// half_area_x2 of a box; empty != 0 takes Aabb::EMPTY instead of (mn, mx).
+float oracle_box_half_area_x2(const float mn[3], const float mx[3], int empty) {
+    return (empty ? Aabb::empty() : Aabb{v3_at(mn), v3_at(mx)}).half_area_x2();
+}
+// Whether the box of two corner points overlaps the box around a sphere.
+int oracle_box_sphere_overlap(const float a[3], const float b[3], const float center[3], float radius) {
+    Aabb box = Aabb::empty().grow(v3_at(a)).grow(v3_at(b));
+    return box.intersects(Aabb::from_sphere(v3_at(center), radius)) ? 1 : 0;
+}
+float oracle_triangle_area(const float tri[9]) { return triangle_area(v3_at(tri), v3_at(tri + 3), v3_at(tri + 6)); }
+int oracle_approx_eq(const float a[3], const float b[3], float eps) { return approx_eq(v3_at(a), v3_at(b), eps) ? 1 : 0; }
+
+// ---- light_shape.rs helpers (light_shape.rs:22-65) ----
+float oracle_light_reach(const dl_light *l) { return Light{l}.shape_reach(); }
+uint32_t oracle_light_shadow_bits(const dl_light *l) { return Light{l}.shadow_bits(); }
+int oracle_light_may_face(const dl_light *l, const float tri[9], const float normal[3]) {
+    V3 v[3] = {v3_at(tri), v3_at(tri + 3), v3_at(tri + 6)};
+    return Light{l}.may_face(v, v3_at(normal)) ? 1 : 0;
+}
+
+// ---- shadows.rs helpers (shadows.rs:136-160): a region of `w` x `h` levels over `rect` ----
+static ShadowRegion region_of(const uint8_t *levels, uint32_t w, uint32_t h, uint32_t bits, const uint32_t rect[4]) {
+    ShadowRegion r{Rect{rect[0], rect[1], rect[2], rect[3]}, ShadowGrid(w, h, bits)};
+    for (uint32_t y = 0; y < h; ++y)
+        for (uint32_t x = 0; x < w; ++x) r.grid.set(x, y, levels[(size_t)y * w + x]);
+    return r;
+}
+// The padded, dilated grid of `crop`: (crop width + 4) x (crop height + 4) levels into `out`.
+void oracle_crop_shadows(const uint8_t *levels, uint32_t w, uint32_t h, uint32_t bits, const uint32_t rect[4],
+                         const uint32_t crop[4], uint8_t *out) {
+    ShadowGrid g = crop_shadows(region_of(levels, w, h, bits, rect), Rect{crop[0], crop[1], crop[2], crop[3]});
+    std::memcpy(out, g.levels.data(), g.levels.size());
+}
+int oracle_any_light(const uint8_t *levels, uint32_t w, uint32_t h, uint32_t bits, const uint32_t rect[4],
+                     const uint32_t query[4]) {
+    return any_light(region_of(levels, w, h, bits, rect), Rect{query[0], query[1], query[2], query[3]}) ? 1 : 0;
+}
+
 }  // extern "C"

@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 import dynlight_gb300 as dl
+from dynlight_gb300 import scenes
 from oracle import oracle as orc
 from oracle.oracle import f32, ptr
 
@@ -626,3 +627,121 @@ def test_orthonormal_pair_and_rotation():
     r = (C.c_float * 3)()
     L.oracle_quat_rotate(ptr(f32(*dl.scenes.rotation_x(-math.pi / 2))), ptr(f32(0, 0, 1)), r)
     assert np.allclose(list(r), [0, 1, 0], atol=1e-6)  # a sun turned down is above (shape.rs:152-161)
+
+
+def v3(*x):
+    return ptr(f32(*x))
+
+
+def test_closest_point_covers_every_region():
+    # src/bake/geometry.rs:159-189: the seven Voronoi regions of a right triangle in z = 0
+    tri = f32(0, 0, 0, 1, 0, 0, 0, 1, 0)
+    cases = [((0.25, 0.25, 1.0), (0.25, 0.25, 0.0)), ((-1.0, -1.0, 0.0), (0, 0, 0)), ((2.0, -0.5, 0.0), (1, 0, 0)),
+             ((-0.5, 2.0, 0.0), (0, 1, 0)), ((0.5, -1.0, 0.0), (0.5, 0.0, 0.0)), ((-1.0, 0.5, 0.0), (0.0, 0.5, 0.0)),
+             ((1.0, 1.0, 0.0), (0.5, 0.5, 0.0))]
+    out = np.zeros(3, np.float32)
+    for p, want in cases:
+        L.oracle_closest_point(v3(*p), ptr(tri), ptr(out))
+        assert np.all(np.abs(out - np.float32(want)) <= 1e-6), (p, out)
+    L.oracle_sphere_triangle.argtypes = [C.c_void_p, C.c_float, C.c_void_p]
+    assert L.oracle_sphere_triangle(v3(0.2, 0.2, 0.5), 0.5, ptr(tri)) == 1
+    assert L.oracle_sphere_triangle(v3(0.2, 0.2, 0.6), 0.5, ptr(tri)) == 0
+
+
+def test_barycentrics_detect_outside_points_and_both_windings():
+    # src/bake/geometry.rs:191-201
+    w = np.zeros(3, np.float32)
+    assert L.oracle_uv_barycentrics(ptr(f32(0, 0, 1, 0, 0, 1)), ptr(f32(0.25, 0.25)), ptr(w)) == 1
+    assert np.all(np.abs(w - np.float32([0.5, 0.25, 0.25])) <= 1e-6)
+    assert L.oracle_uv_barycentrics(ptr(f32(0, 0, 1, 0, 0, 1)), ptr(f32(0.75, 0.75)), ptr(w)) == 0
+    assert L.oracle_uv_barycentrics(ptr(f32(0, 0, 0, 1, 1, 0)), ptr(f32(0.25, 0.25)), ptr(w)) == 1
+    assert np.all(np.abs(w - np.float32([0.5, 0.25, 0.25])) <= 1e-6), "the flipped winding"
+    assert L.oracle_uv_barycentrics(ptr(f32(0, 0, 1, 0, 2, 0)), ptr(f32(1, 0)), ptr(w)) == 0, "degenerate"
+
+
+def test_boxes_and_areas():
+    # src/bake/geometry.rs:203-215
+    L.oracle_box_sphere_overlap.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float]
+    L.oracle_box_half_area_x2.restype = C.c_float
+    L.oracle_triangle_area.restype = C.c_float
+    L.oracle_approx_eq.argtypes = [C.c_void_p, C.c_void_p, C.c_float]
+    assert L.oracle_box_sphere_overlap(v3(0, 0, 0), v3(1, 1, 1), v3(2, 2, 2), 1.0) == 1, "touching boxes overlap"
+    assert L.oracle_box_sphere_overlap(v3(0, 0, 0), v3(1, 1, 1), v3(2, 2, 2), 0.9) == 0
+    assert L.oracle_box_half_area_x2(v3(0, 0, 0), v3(1, 1, 1), 0) == 6.0
+    assert L.oracle_box_half_area_x2(v3(0, 0, 0), v3(0, 0, 0), 1) == 0.0, "the empty box"
+    assert L.oracle_triangle_area(ptr(f32(0, 0, 0, 2, 0, 0, 0, 2, 0))) == 2.0
+    assert L.oracle_approx_eq(v3(0, 1, 0), v3(0, 1.000001, 0), 1e-5) == 1
+    assert L.oracle_approx_eq(v3(0, 1, 0), v3(0, -1, 0), 1e-5) == 0
+
+
+class OneLight:
+    """A BakeLight marshalled as a dl_light for the oracle's light helpers."""
+
+    def __init__(self, light):
+        self.m = dl.Marshalled(dl.BakeInput([], [light]))
+        self.p = self.m.input.lights
+        L.oracle_light_reach.restype = C.c_float
+
+    def reach(self):
+        return L.oracle_light_reach(self.p)
+
+    def bits(self):
+        return L.oracle_light_shadow_bits(self.p)
+
+    def may_face(self, tri, normal):
+        return L.oracle_light_may_face(self.p, ptr(f32(*np.ravel(tri))), v3(*normal)) == 1
+
+
+def test_area_lights_reach_and_face_with_their_shape():
+    # src/bake/light_shape.rs:77-113
+    point = OneLight(fx.point_light(1, (0, 2, 0), 3.0))
+    assert (point.reach(), point.bits()) == (3.0, 1)
+    tube = OneLight(fx.area_light(1, (0, 2, 0), 5.0, (0.0, 0.0, 0.0, 1.0), (4.0, 0.0)))
+    assert (tube.reach(), tube.bits()) == (3.0, 4)
+    wall = np.float32([[1.5, 0, 0], [1.5, 1, 0], [1.5, 0, 1]])
+    assert tube.may_face(wall, (1, 0, 0)), "a wall at x = 1.5 facing +X sees the tube's far end"
+    assert not tube.may_face(wall + np.float32([1, 0, 0]), (1, 0, 0))
+    panel = OneLight(fx.area_light(1, (0, 2, 0), 5.0, scenes.rotation_x(-math.pi / 2), (1.0, 1.0)))
+    floor = np.float32([[0, 0, 0], [0, 0, 1], [1, 0, 0]])
+    assert not panel.may_face(floor + np.float32([0, 3, 0]), (0, 1, 0)), "above a downward panel: its dark side"
+    assert panel.may_face(floor, (0, 1, 0))
+
+
+def test_suns_face_by_direction_and_soften_with_their_disk():
+    # src/bake/light_shape.rs:114-131
+    floor = np.float32([[0, 0, 0], [0, 0, 1], [1, 0, 0]])
+    low = OneLight(fx.sun_light(1, (1.0, 0.02, 0.0), 0.0))
+    assert low.bits() == 1, "no disk, hard shadows"
+    assert low.may_face(floor, (0, 1, 0))
+    assert low.may_face(floor, (0, -1, 0)), "within Henry's tolerance"
+    assert not low.may_face(floor, (-1, 0, 0))
+    below = np.float32([1.0, -0.11, 0.0])
+    below = below / np.float32(np.linalg.norm(below))
+    assert not OneLight(fx.sun_light(2, below, 0.0)).may_face(floor, (0, 1, 0))
+    wide = OneLight(fx.sun_light(2, below, 10.0))
+    assert wide.may_face(floor, (0, 1, 0)), "the top of a wide disk still reaches the floor"
+    assert wide.bits() == 4
+
+
+def test_crops_offset_by_two_and_dilate():
+    # src/bake/shadows.rs:174-191
+    for bits in (1, 4):
+        levels = np.zeros((10, 10), np.uint8)
+        levels[5, 4] = 1
+        out = np.zeros(7 * 6, np.uint8)
+        L.oracle_crop_shadows(ptr(levels), 10, 10, bits, ptr(np.uint32([0, 0, 9, 9])), ptr(np.uint32([4, 5, 6, 6])),
+                              ptr(out))
+        g = out.reshape(6, 7)
+        assert g[2, 2] == 1, "texel (4, 5) lands at (2, 2)"
+        assert (g[0, 0], g[1, 1]) == (1, 1), "dilated"
+        assert g[3, 3] == 0, "interior texels are not dilated"
+
+
+def test_any_light_only_looks_inside_both_rects():
+    # src/bake/shadows.rs:193-205
+    levels = np.zeros((4, 4), np.uint8)
+    levels[3, 3] = 2
+    region = ptr(np.uint32([10, 10, 13, 13]))
+    hits = [L.oracle_any_light(ptr(levels), 4, 4, 4, region, ptr(np.uint32(q)))
+            for q in ([12, 12, 20, 20], [0, 0, 12, 12], [0, 0, 5, 5])]
+    assert hits == [1, 0, 0]
