@@ -1342,6 +1342,21 @@ void oracle_slerp(const float a[3], const float b[3], float s, float out[3]) {
     out[0] = r.x; out[1] = r.y; out[2] = r.z;
 }
 
+// ---- random streams (effects/rng.rs:27-93, random.rs:8-28) ----
+// `count` values of EffectRng::new(seed, stream).
+void oracle_rng_u32(uint64_t seed, uint64_t stream_id, uint32_t count, uint32_t *out) {
+    Rng r = rng_new(seed, stream_id);
+    for (uint32_t i = 0; i < count; ++i) out[i] = r.next_u32();
+}
+// `count` points of on_unit_sphere from the keyed stream of `parts`.
+void oracle_sphere_points(const uint64_t *parts, int n, uint32_t count, float *out) {
+    Rng r = stream(parts, n);
+    for (uint32_t i = 0; i < count; ++i) {
+        V3 p = on_unit_sphere(r);
+        out[i * 3] = p.x; out[i * 3 + 1] = p.y; out[i * 3 + 2] = p.z;
+    }
+}
+
 // ---- geometry.rs helpers (geometry.rs:19-140) ----
 static V3 v3_at(const float *p) { return V3{p[0], p[1], p[2]}; }
 void oracle_closest_point(const float p[3], const float tri[9], float out[3]) {

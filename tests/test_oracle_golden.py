@@ -745,3 +745,45 @@ def test_any_light_only_looks_inside_both_rects():
     hits = [L.oracle_any_light(ptr(levels), 4, 4, 4, region, ptr(np.uint32(q)))
             for q in ([12, 12, 20, 20], [0, 0, 12, 12], [0, 0, 5, 5])]
     assert hits == [1, 0, 0]
+
+
+def rng_u32(seed, stream_id, count):
+    out = np.zeros(count, np.uint32)
+    L.oracle_rng_u32.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, C.c_void_p]
+    L.oracle_rng_u32(seed, stream_id, count, ptr(out))
+    return out
+
+
+def for_light(seed, key, count):
+    """EffectRng::for_light(seed, key) (src/effects/rng.rs:33-35): `count` u32 values."""
+    sm = dl.scenes.splitmix64
+    return rng_u32(sm(seed ^ sm(key)), key, count)
+
+
+def test_pcg_streams_repeat_per_seed_and_differ_between_lights():
+    # src/effects/rng.rs:96-107
+    a, b, c = for_light(7, 1, 16), for_light(7, 1, 16), for_light(7, 2, 16)
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+
+
+def test_pcg_floats_are_uniform_in_the_unit_interval():
+    # src/effects/rng.rs:108-122: next_f32 = (u32 >> 8) * 2^-24
+    values = (for_light(1, 99, 100_000) >> 8).astype(np.float32) * np.float32(1.0 / 16777216.0)
+    assert values.min() >= 0.0 and values.max() < 1.0
+    shares = np.bincount((values * np.float32(10.0)).astype(int), minlength=10) / values.size
+    assert np.all(np.abs(shares - 0.1) < 0.01), shares
+
+
+def test_splitmix_spreads_neighbouring_inputs():
+    # src/effects/rng.rs:156-160
+    sm = dl.scenes.splitmix64
+    assert 16 <= bin(sm(1) ^ sm(2)).count("1") <= 48
+
+
+def test_sphere_points_are_unit_and_centered():
+    # src/bake/random.rs:41-51: 20 000 points of the keyed stream [7]
+    out = np.zeros(3 * 20_000, np.float32)
+    L.oracle_sphere_points(ptr(np.uint64([7])), 1, 20_000, ptr(out))
+    p = out.reshape(-1, 3).astype(np.float64)
+    assert np.all(np.abs(np.linalg.norm(p, axis=1) - 1.0) < 1e-4)
+    assert np.linalg.norm(p.mean(axis=0)) < 0.02
