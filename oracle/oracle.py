@@ -1,8 +1,8 @@
 """TEST INFRASTRUCTURE — ctypes binding of the parity oracle (oracle/_build/liboracle.so).
 
 The oracle is a C++ restatement of the reference CPU baker. Only the tests, the smoke check
-and the benchmark's CPU-baseline leg use it, always as the checker or the timed CPU baseline,
-never as a path of the product.
+and the benchmark's CPU-baseline leg use it: as what the library's outputs are compared with,
+or as the timed CPU baseline, never as a path of the product.
 """
 import ctypes as C
 import os

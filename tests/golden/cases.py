@@ -190,7 +190,7 @@ CASES = {
 
 
 def oracle_bake(name, threads=0):
-    """The oracle's bake of case `name` (the checker side of the fixtures)."""
+    """The oracle's bake of case `name` (the side of the fixtures that outputs are compared with)."""
     from oracle import oracle
     inp, opts, form = CASES[name]()
     if form == "refined":

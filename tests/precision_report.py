@@ -13,7 +13,7 @@
    FP64 oracle, for the refined form at epsilon 1e-7, 1e-6, 1e-5 and 1e-4.
 With --outdoor: the full 546k-triangle outdoor scene, every GPU form against both oracles.
 
-Test infrastructure: the oracle is the checker here, never a path of the product.
+Test infrastructure: the oracle is what the GPU forms are compared with here, never a path of the product.
 """
 import argparse
 import json

@@ -16,7 +16,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 @pytest.fixture(scope="module")
-def checker(tmp_path_factory):
+def bvh_tool(tmp_path_factory):
     exe = tmp_path_factory.mktemp("native") / "light_bvh_check"
     csrc = os.path.join(ROOT, "dynamiclighting-bevy_gb300", "csrc")
     subprocess.run(["g++", "-O2", "-std=c++17", "-pthread", "-ffp-contract=off", "-fno-fast-math", "-x", "c++",
@@ -43,10 +43,10 @@ def light_set(kind, n, seed):
     return np.float32(pos), np.float32(rad)
 
 
-def library_bvh(checker, tmp_path, pos, rad):
+def library_bvh(bvh_tool, tmp_path, pos, rad):
     src, dst = tmp_path / "lights.bin", tmp_path / "bvh.bin"
     src.write_bytes(np.uint32([len(rad)]).tobytes() + np.concatenate([pos, rad[:, None]], 1).astype(np.float32).tobytes())
-    subprocess.run([str(checker), str(src), str(dst)], check=True)
+    subprocess.run([str(bvh_tool), str(src), str(dst)], check=True)
     data = np.frombuffer(dst.read_bytes(), np.uint32)
     count = int(data[0])
     return data[1:1 + 8 * count].reshape(count, 8), data[1 + 8 * count:]
@@ -63,9 +63,9 @@ def oracle_bvh(pos, rad):
 
 @pytest.mark.parametrize("kind", ["uniform", "clusters", "coincident", "radii"])
 @pytest.mark.parametrize("n", [1, 2, 7, 64, 513, 2000])
-def test_host_light_bvh_equals_the_oracle(checker, tmp_path, kind, n):
+def test_host_light_bvh_equals_the_oracle(bvh_tool, tmp_path, kind, n):
     pos, rad = light_set(kind, n, seed=1000 * n + len(kind))
-    nodes, order = library_bvh(checker, tmp_path, pos, rad)
+    nodes, order = library_bvh(bvh_tool, tmp_path, pos, rad)
     want_nodes, want_order = oracle_bvh(pos, rad)
     assert np.array_equal(order, want_order)
     assert nodes.shape == want_nodes.shape and np.array_equal(nodes, want_nodes)
