@@ -3189,7 +3189,10 @@ dl_status dl_session_encode_payload(dl_session *s, uint8_t **bytes, uint64_t *le
 }
 
 dl_status dl_session_report(const dl_session *s, dl_bake_report *report) {
-    if (!s || !report) return DL_INVALID_ARGUMENT;
+    if (!s || !report) {
+        g_error = "null argument";
+        return DL_INVALID_ARGUMENT;
+    }
     *report = s->report;
     return DL_OK;
 }
@@ -3245,17 +3248,24 @@ dl_status dl_bake(const dl_bake_input *input, const dl_bake_options *options, dl
 }
 
 dl_status dl_encode_payload(const dl_baked_scene *scene, uint8_t **bytes, uint64_t *length, uint32_t *crc) {
-    if (!scene || !bytes || !length) return DL_INVALID_ARGUMENT;
+    if (!scene || !bytes || !length) {
+        g_error = "null argument";
+        return DL_INVALID_ARGUMENT;
+    }
     try {
         std::vector<uint8_t> p = encode_payload(*scene);
         uint8_t *b = static_cast<uint8_t *>(std::malloc(p.size() ? p.size() : 1));
-        if (!b) return DL_OUT_OF_MEMORY;
+        if (!b) {
+            g_error = "host allocation failed";
+            return DL_OUT_OF_MEMORY;
+        }
         if (!p.empty()) std::memcpy(b, p.data(), p.size());
         *bytes = b;
         *length = p.size();
         if (crc) *crc = crc32_ieee(p.data(), p.size());
         return DL_OK;
     } catch (...) {
+        g_error = "host allocation failed";
         return DL_OUT_OF_MEMORY;
     }
 }

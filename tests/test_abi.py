@@ -53,3 +53,33 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
     monkeypatch.setattr(dl, "_LIB", None)
     with pytest.raises(RuntimeError, match="not built"):
         dl.load_library(str(tmp_path / "nope.so"))
+
+
+def test_argument_errors_are_named_without_a_gpu():
+    """Entry points reject null or out-of-range arguments before any CUDA call, with a status and
+    a message in dl_last_error (the C ABI's form of the reference's BakeError text)."""
+    if not os.path.exists(dl.LIBRARY_PATH):
+        pytest.skip("library not built (run __graft_entry__.build())")
+    lib = C.CDLL(dl.LIBRARY_PATH)
+    lib.dl_last_error.restype = C.c_char_p
+    invalid_argument = 21
+    null = C.c_void_p()
+    n, crc = C.c_uint64(), C.c_uint32()
+    assert lib.dl_encode_payload(null, C.byref(null), C.byref(n), C.byref(crc)) == invalid_argument
+    assert lib.dl_last_error() == b"null argument"
+    assert lib.dl_session_report(null, null) == invalid_argument
+    assert lib.dl_last_error() == b"null argument"
+    assert lib.dl_session_create(null, null, null, C.byref(null)) == invalid_argument
+    assert lib.dl_last_error() == b"null argument"
+    assert lib.dl_session_run(null, null) == invalid_argument
+    assert lib.dl_last_error() == b"null session"
+    # the non-allocating filter checks its window before it touches a device
+    buf_a, buf_b = (C.c_float * 3)(), (C.c_float * 3)()
+    args = (C.c_uint32(0), C.c_uint32(1), C.c_uint32(0), C.c_uint32(0), C.c_uint32(4), null)
+    assert lib.dl_filter_bounce_window_noalloc(buf_a, buf_b, *args) == invalid_argument
+    assert b"texels" in lib.dl_last_error()
+    args = (C.c_uint32(1), C.c_uint32(1), C.c_uint32(4), C.c_uint32(0), C.c_uint32(4), null)
+    assert lib.dl_filter_bounce_window_noalloc(buf_a, buf_b, *args) == invalid_argument
+    assert lib.dl_last_error() == b"the window does not lie inside the map"
+    assert lib.dl_filter_bounce_window_noalloc(buf_a, buf_a, *args) == invalid_argument
+    assert b"distinct" in lib.dl_last_error()
