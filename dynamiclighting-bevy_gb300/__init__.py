@@ -12,6 +12,7 @@ the library is not built the call fails loudly with the build command to run.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 from dataclasses import dataclass, field
 from typing import List, Optional, Sequence
@@ -181,6 +182,98 @@ class BakeProgress:
 def _f32(a, cols):
     a = np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1, cols))
     return a
+
+
+def _hex_id(i):
+    """A BakeId as the library's messages print it (C's %#018llx)."""
+    return f"{i:#018x}" if i else "0" * 18
+
+
+def _options_error(o: BakeOptions):
+    """BakeOptions::validate (src/bake/input.rs:336-373) with the library's messages."""
+    bad = None
+    if not (math.isfinite(o.pixel_density) and o.pixel_density > 0.0):
+        bad = "pixel density must be positive"
+    elif o.max_lightmap_size < 2:
+        bad = "the maximum shadow map size must be at least 2"
+    elif o.photon_cube_resolution == 0:
+        bad = "the photon cube resolution must be positive"
+    elif o.area_light_samples == 0:
+        bad = "area lights need at least one sample"
+    elif not 1 <= o.sun_map_resolution <= 8192:
+        bad = "the sun map resolution must be 1 to 8192"
+    elif o.sky_samples == 0:
+        bad = "skies need at least one sample"
+    elif not (math.isfinite(o.sky_probe_spacing) and o.sky_probe_spacing > 0.0):
+        bad = "the sky probe spacing must be positive"
+    elif o.bounce_compression not in (8, 6, 5, 4):
+        bad = "bounce compression must be 8, 6, 5 or 4 bits"
+    elif o.dynamic_geometry > ANGULAR:
+        bad = "unknown dynamic geometry mode"
+    return None if bad is None else "invalid bake options: " + bad
+
+
+def _mesh_error(m: BakeMesh):
+    """BakeMesh::validate (src/bake/input.rs:233-284) in the reference's order. Returns
+    (reason, length_rule): length_rule marks the rules the C ABI cannot check, because a dl_mesh
+    carries one vertex count for all of its arrays."""
+    idx = np.asarray(m.indices, dtype=np.uint32).reshape(-1)
+    pos = np.asarray(m.positions, dtype=np.float32).reshape(-1, 3)
+    v = pos.shape[0]
+    if len(idx) % 3:
+        return f"{len(idx)} indices is not a multiple of 3", False
+    if len(idx) and int(idx.max()) >= v:
+        return f"index {int(idx[np.argmax(idx >= v)])} is out of range for {v} vertices", False
+    n_uv1 = np.asarray(m.uv1, dtype=np.float32).reshape(-1, 2).shape[0]
+    if n_uv1 != v:
+        return f"{n_uv1} UV1 coordinates for {v} vertices", True
+    if m.normals is not None and len(m.normals):
+        n_nrm = np.asarray(m.normals, dtype=np.float32).reshape(-1, 3).shape[0]
+        if n_nrm != v:
+            return f"{n_nrm} normals for {v} vertices", True
+    if not np.isfinite(pos).all():
+        return "non-finite vertex position", False
+    if m.uv0 is not None:
+        n_uv0 = np.asarray(m.uv0, dtype=np.float32).reshape(-1, 2).shape[0]
+        if n_uv0 != v:
+            return f"{n_uv0} UV0 coordinates for {v} vertices", True
+    if m.alpha is not None:
+        if m.uv0 is None:
+            return "an alpha texture needs UV0", False
+        if np.asarray(m.alpha.rgba8, dtype=np.uint8).size != m.alpha.width * m.alpha.height * 4:
+            return "alpha texture size doesn't match its data", True
+    return None, False
+
+
+def _lengths_disagree(m: BakeMesh):
+    """Whether a per-vertex array or the alpha texture's data disagrees with the mesh's sizes."""
+    v = np.asarray(m.positions).size // 3
+    rows = lambda a, k: np.asarray(a).size // k  # noqa: E731
+    return (rows(m.uv1, 2) != v or (m.normals is not None and len(m.normals) and rows(m.normals, 3) != v)
+            or (m.uv0 is not None and rows(m.uv0, 2) != v)
+            or (m.alpha is not None and np.asarray(m.alpha.rgba8).size != m.alpha.width * m.alpha.height * 4))
+
+
+def _check_array_lengths(inp: BakeInput, options: BakeOptions):
+    """Raises the reference's error for an input whose arrays disagree in length with its
+    positions. The C ABI reads every per-vertex array with the mesh's one vertex count, so such an
+    input must not reach it. When no length rule fails, this does nothing and the library checks
+    everything else. Otherwise the whole validation runs here in the reference's order (options,
+    duplicate mesh ids, then each mesh in id order; src/bake/baker.rs:32-35,205-218), so the first
+    error reported is the reference's."""
+    if not any(_lengths_disagree(m) for m in inp.meshes):
+        return
+    err = _options_error(options)
+    if err:
+        raise BakeError(5, err)
+    meshes = sorted(inp.meshes, key=lambda m: int(m.id))
+    for a, b in zip(meshes, meshes[1:]):
+        if int(a.id) == int(b.id):
+            raise BakeError(2, "two meshes share BakeId " + _hex_id(int(b.id)))
+    for m in meshes:
+        reason, _ = _mesh_error(m)
+        if reason:
+            raise BakeError(3, f"mesh {_hex_id(int(m.id))}: {reason}")
 
 
 class Marshalled:
@@ -450,6 +543,7 @@ def bake(inp: BakeInput, options: BakeOptions, progress: Optional[BakeProgress] 
          form="batched", report: Optional[DlBakeReport] = None, **tuning) -> BakedScene:
     """bake() (src/bake/baker.rs:27-31) on the GPU through dl_bake_ex."""
     lib = load_library()
+    _check_array_lengths(inp, options)
     m = Marshalled(inp)
     opts = marshal_options(options)
     cfg = make_config(form, **tuning)
@@ -471,6 +565,7 @@ class Session:
 
     def __init__(self, inp: BakeInput, options: BakeOptions, form="batched", **tuning):
         self.lib = load_library()
+        _check_array_lengths(inp, options)
         self._m = Marshalled(inp)
         self._opts = marshal_options(options)
         self._cfg = make_config(form, **tuning)
