@@ -156,3 +156,14 @@ def test_invalid_tuning_is_an_argument_error():
     inp, opts = room()
     fails(inp, opts, "invalid argument", "sample_lanes", sample_lanes=3)
     fails(inp, opts, "invalid argument", "refine_epsilon", refine_epsilon=0.5)
+
+
+@pytest.mark.parametrize("mesh_id", [0, 1, 0xFFFFFFFFFFFFFFFF])
+def test_ids_print_as_the_library_prints_them(mesh_id):
+    # a duplicate id reported by the library, then by the mirror (a length fault elsewhere)
+    inp, opts = room()
+    inp.meshes[0].id = inp.meshes[1].id = mesh_id
+    from_library = fails(inp, opts, "DuplicateId", "two meshes share BakeId")
+    inp.meshes[2].uv1 = inp.meshes[2].uv1[:-1]
+    assert fails(inp, opts, "DuplicateId", "two meshes share BakeId") == from_library
+    assert from_library.endswith(dl._hex_id(mesh_id))
