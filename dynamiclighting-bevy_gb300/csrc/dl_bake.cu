@@ -1630,7 +1630,11 @@ void wait(dl_session &s, dl_progress *progress) {
     }
 }
 
-dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bake_config *cfg, dl_session *&out) {
+// `progress`, when given, is checked for cancellation once validation has passed and before the
+// first CUDA call: as in the reference (baker.rs:32-55), invalid input reports its own error even
+// when the bake was already cancelled.
+dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bake_config *cfg, dl_session *&out,
+                 const dl_progress *progress = nullptr) {
     auto s = std::make_unique<dl_session>();
     s->options = *o;
     if (cfg) s->config = *cfg;
@@ -1662,6 +1666,10 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
             g_error = "shadow maps larger than 65535 texels per side are not supported";
             return DL_UNSUPPORTED;
         }
+    if (progress && progress->cancel) {
+        g_error = "the bake was cancelled";
+        return DL_CANCELLED;
+    }
     s->report.ms_host[0] = ms_since(t_prep);
     // the occluder BVH: on the host's cores when asked, else on the device once the triangles
     // are uploaded (the same tree)
@@ -3007,6 +3015,25 @@ dl_status result(dl_session &s, dl_baked_scene *&out) {
         return DL_CUDA_ERROR;                                                         \
     }
 
+// dl_session_create with an optional progress whose cancel flag create() checks.
+static dl_status session_create(const dl_bake_input *input, const dl_bake_options *options,
+                                const dl_bake_config *config, const dl_progress *progress, dl_session **out) {
+    if (!input || !options || !out) {
+        g_error = "null argument";
+        return DL_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    DL_GUARD({
+        dl_session *s = nullptr;
+        auto t0 = std::chrono::steady_clock::now();
+        dl_status st = create(input, options, config, s, progress);
+        if (st != DL_OK) return st;
+        s->report.ms_upload = ms_since(t0);
+        *out = s;
+        return DL_OK;
+    })
+}
+
 extern "C" {
 
 uint32_t dl_abi_version(void) { return DL_ABI_VERSION; }
@@ -3051,20 +3078,7 @@ void dl_default_options(dl_bake_options *o) {
 
 dl_status dl_session_create(const dl_bake_input *input, const dl_bake_options *options,
                             const dl_bake_config *config, dl_session **out) {
-    if (!input || !options || !out) {
-        g_error = "null argument";
-        return DL_INVALID_ARGUMENT;
-    }
-    *out = nullptr;
-    DL_GUARD({
-        dl_session *s = nullptr;
-        auto t0 = std::chrono::steady_clock::now();
-        dl_status st = create(input, options, config, s);
-        if (st != DL_OK) return st;
-        s->report.ms_upload = ms_since(t0);
-        *out = s;
-        return DL_OK;
-    })
+    return session_create(input, options, config, nullptr, out);
 }
 
 dl_status dl_session_run(dl_session *s, dl_progress *progress) {
@@ -3219,15 +3233,9 @@ dl_status dl_bake_ex(const dl_bake_input *input, const dl_bake_options *options,
         return DL_BUSY;
     }
     auto t0 = std::chrono::steady_clock::now();
-    if (progress) {
-        progress->stage = 0;
-        if (progress->cancel) {
-            g_error = "the bake was cancelled";
-            return DL_CANCELLED;
-        }
-    }
+    if (progress) progress->stage = 0;
     dl_session *s = nullptr;
-    dl_status st = dl_session_create(input, options, config, &s);
+    dl_status st = session_create(input, options, config, progress, &s);
     if (st != DL_OK) return st;
     std::unique_ptr<dl_session> owner(s);
     st = dl_session_run(s, progress);

@@ -131,7 +131,9 @@ typedef struct dl_bake_options {
 } dl_bake_options;
 
 /* BakeProgress (src/bake/progress.rs:41-110). The caller may set `cancel` from any thread;
- * the library polls it between stages and the device work queue stops at its next item. */
+ * the library polls it between stages and the device work queue stops at its next item. It is
+ * first read after validation, as in the reference (src/bake/baker.rs:32-55): invalid input
+ * reports its own error even when the flag was set before the call. */
 typedef struct dl_progress {
     volatile uint32_t cancel;
     volatile uint32_t stage; /* BakeStage order (src/bake/progress.rs:8-16) */

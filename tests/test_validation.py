@@ -167,3 +167,20 @@ def test_ids_print_as_the_library_prints_them(mesh_id):
     inp.meshes[2].uv1 = inp.meshes[2].uv1[:-1]
     assert fails(inp, opts, "DuplicateId", "two meshes share BakeId") == from_library
     assert from_library.endswith(dl._hex_id(mesh_id))
+
+
+def test_a_cancelled_bake_reports_cancelled_after_validation():
+    # progress.check() follows validation in the reference (baker.rs:32-55): invalid input reports
+    # its own error even when the bake was cancelled before it started; valid input is cancelled
+    # before the library touches a device
+    inp, opts = room()
+    progress = dl.BakeProgress()
+    progress.cancel()
+    fails(inp, opts, "Cancelled", "the bake was cancelled", progress=progress)
+    assert progress.stage == 0
+    fails(inp, dataclasses.replace(opts, pixel_density=0.0), "InvalidOptions", "pixel density", progress=progress)
+    inp.lights[0].id = inp.lights[1].id
+    fails(inp, opts, "DuplicateId", "two lights share BakeId", progress=progress)
+    inp, opts = room()
+    inp.meshes[0].uv1 = inp.meshes[0].uv1[:-1]
+    fails(inp, opts, "InvalidMesh", "UV1 coordinates", progress=progress)
