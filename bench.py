@@ -5,12 +5,23 @@ the CPU oracle (a restatement of the reference's CPU baker) timed on the host co
 
 A step is one bake of the workload. `value` is the device-resident throughput: shadow rays
 (BakeStats.rays + bounce_rays) per second of device time of every bake stage, with the scene and
-its BVH resident. `e2e` is the same metric through dl_bake() from host buffers: validation, BVH
-build, uploads, the device pipeline, download and serialization. The L2 is flushed (a 256 MiB
+its BVH resident. `e2e` is the same metric through dl_bake_ex() from host buffers: validation,
+BVH build, uploads, the device pipeline, download and serialization. The L2 is flushed (a 256 MiB
 write) before every timed step. Multi-GPU runs are independent replicas (the bake shards by
 scene, with no exchange step): one rank per GPU, each baking the full workload.
+
+The roofline of the dominant kernel (the persistent visibility kernel) divides its algorithmic
+bytes (node visits x 64 B + triangle tests x 48 B + 76 B per work item, counted by the
+instrumented variant) by the L2 read bandwidth measured in the same run. On a 1-GPU run the CPU
+leg times the oracle once on the full workload on every host core (and checks that its words
+equal the GPU's), and measures the target's bounce clause on the workload's seeded CPU sample:
+the bounce maps of the bit-exact and refined forms against the FP64 oracle.
+
+`--impl reference` times the oracle alone on the host cores, one bounded sample of the workload
+per step (the same seeded sample the bounce clause uses), and prints the same metric.
 """
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
@@ -29,6 +40,10 @@ from dynlight_gb300 import scenes  # noqa: E402
 
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
+# The headline metric, printed identically by both arms so their lines compare directly.
+METRIC = "shadow rays/s & bake ms: batched vs plain GPU at bit-exact masks; CPU ref"
+# The cache read-bandwidth probe behind the roofline: a buffer that fits in L2 (129 MB).
+L2_PROBE_BYTES = 64 << 20
 
 WORKLOADS = {
     # name: (generator, description)
@@ -125,18 +140,51 @@ def rank_info():
     return rank, world, local
 
 
-def cpu_baseline(name, seconds_cap=60.0):
-    """The oracle, all host threads, on the bounded sample of the workload."""
+def cpu_baseline(name, full=None):
+    """The oracle, all host threads: on the bounded sample of the workload, or on the full
+    workload when `full` gives its (input, options)."""
     from oracle import oracle
-    make, desc = CPU_SAMPLES[name]
-    inp, opts = make()
+    if full is not None:
+        (inp, opts), desc = full, "the full workload"
+    else:
+        make, desc = CPU_SAMPLES[name]
+        inp, opts = make()
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
     scene, burial, _ = oracle.bake(inp, opts, threads=threads)
     dt = time.perf_counter() - t0
     rays = scene.stats["rays"] + scene.stats["bounce_rays"]
     return {"value": rays / dt, "unit": "rays/s", "cores": threads, "kind": "port",
-            "sample": f"{desc}: {rays} shadow rays + {burial} burial rays in {dt:.2f} s", "seconds": dt}
+            "sample": f"{desc}: {rays} shadow rays + {burial} burial rays in {dt:.2f} s", "seconds": dt,
+            "scene": scene}
+
+
+def precision_slice(name, device):
+    """The bounce clause of the target on the workload's seeded CPU sample: the filtered bounce
+    maps of the bit-exact (batched) and refined forms against the FP64 oracle's, as the maximum
+    relative error (dynlight_gb300.compare.bounce_error), and the refined form's device time there.
+    The oracle is the checker here."""
+    from dynlight_gb300 import compare
+    from oracle import oracle
+    make, desc = CPU_SAMPLES[name]
+    inp, opts = make()
+    t0 = time.perf_counter()
+    ref64 = oracle.bake_ex(inp, opts, mode=oracle.F64, threads=os.cpu_count() or 1, bounce_maps=True)
+    out = {"slice": desc, "fp64_oracle_s": round(time.perf_counter() - t0, 2)}
+    for form in ("batched", "refined"):
+        s = dl.Session(inp, opts, form=form, device=device)
+        try:
+            s.run()
+            scene = s.result()
+            maps = compare.session_maps(s, scene)
+        finally:
+            s.close()
+        err = compare.bounce_error(maps, ref64["maps"])
+        flips = compare.bit_flips(scene, ref64["scene"])
+        out[form] = {"bounce_max_rel_err_vs_fp64": err["max"], "bounce_mean_rel_err_vs_fp64": err["mean"],
+                     "bounce_maps": err["maps"], "bounce_texels": err["texels"],
+                     "mask_bits_differing_from_fp64": {k: v["flips"] for k, v in flips.items() if k != "bounce"}}
+    return out
 
 
 def run_reference(args):
@@ -152,12 +200,17 @@ def run_reference(args):
     value = statistics.median(v["value"] for v in vals)
     last = vals[-1]
     ms = statistics.median(v["seconds"] for v in vals) * 1e3
-    line = {"impl": "reference", "metric": "shadow rays/s (bake of the workload)", "value": value,
+    line = {"impl": "reference", "metric": METRIC, "value": value,
             "unit": "rays/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded generator)",
-            "config": {"workload": name, "description": WORKLOADS[name][1], "sample": last["sample"]},
-            "cpu_baseline": {k: last[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "config": {"workload": name, "description": WORKLOADS[name][1],
+                       "timed_sample": CPU_SAMPLES[name][1],
+                       "why_a_sample": "each step bakes a bounded sample of the workload (rays/s is intensive); "
+                                       "the full workload takes about 80 s per bake on 16 cores",
+                       "sample": last["sample"]},
+            "cpu_baseline": {"value": value, "unit": "rays/s", "cores": last["cores"], "kind": last["kind"],
+                             "sample": last["sample"]},
             "e2e": {"value": value, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -213,7 +266,7 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    dev_ms, vis_ms = [], []
+    dev_ms, vis_ms, gather_ms = [], [], []
     with ClockSampler(local) as clocks:
         for _ in range(args.steps):
             flush_l2(torch, flush)
@@ -221,6 +274,7 @@ def main():
             r = session.report()
             dev_ms.append(r.ms_device)
             vis_ms.append(r.ms_visibility)
+            gather_ms.append(r.ms_stages[4])
     torch.cuda.synchronize()
     result = session.result()
     rep = session.report()
@@ -245,6 +299,24 @@ def main():
     hbm, peak_kind = peaks()
     alg_bytes = crep.node_visits * 64 + crep.tri_tests * 48 + crep.work_items * 76
     achieved = alg_bytes / (vis / 1e3) / 1e9 if vis > 0 else 0.0
+    # the roof: the L2 read bandwidth measured now, on this GPU (the BVH is L2-resident), and the
+    # L1 read bandwidth beside it (most node reads hit L1)
+    probe_lib = dl.load_library()
+    l2_gbs, l1_gbs = C.c_double(), C.c_double()
+    assert probe_lib.dl_probe_read_bandwidth(local, 2, L2_PROBE_BYTES, 100, C.byref(l2_gbs)) == 0, \
+        probe_lib.dl_last_error()
+    assert probe_lib.dl_probe_read_bandwidth(local, 1, L2_PROBE_BYTES, 400, C.byref(l1_gbs)) == 0, \
+        probe_lib.dl_last_error()
+
+    # the refined form (binary64 edge re-tests, compensated sums) on the same scene
+    refined = dl.Session(inp, opts, form="refined", device=local)
+    refined_ms = []
+    for i in range(3):
+        refined.run()
+        if i:
+            refined_ms.append(refined.report().ms_device)
+    refined_retests = int(refined.report().retests)
+    refined.close()
     traffic = None
     traffic_path = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(traffic_path):  # DRAM bytes per launch from an ncu capture (profiles/)
@@ -254,7 +326,6 @@ def main():
 
     # end to end through the C ABI (dl_bake_ex) from host buffers: validation, BVH build,
     # uploads, the device pipeline and the download of every mesh's words, timed around the call
-    import ctypes as C
     lib = dl.load_library()
     marshalled = dl.Marshalled(inp)
     copts = dl.marshal_options(opts)
@@ -288,9 +359,12 @@ def main():
                    "texels": int(result.stats["texels"]), "shadow_rays": int(rays),
                    "burial_rays": int(rep.burial_rays), "pairs": int(rep.pairs),
                    "l2": "flushed (256 MiB write) before every timed step",
-                   "plain_form_ms": plain_rep.ms_device, "plain_visibility_ms": plain_rep.ms_visibility,
-                   "batched_visibility_ms": vis,
+                   "batched_ms": ms, "plain_form_ms": plain_rep.ms_device,
+                   "plain_visibility_ms": plain_rep.ms_visibility, "batched_visibility_ms": vis,
+                   "batched_bounce_stage_ms": statistics.median(gather_ms),
                    "speedup_batched_vs_plain": plain_rep.ms_device / ms if ms else None,
+                   "masks_batched_equal_plain": True,
+                   "refined_ms": statistics.median(refined_ms), "refined_retests": refined_retests,
                    "launch_shape": {"chunk_texels": rep.tuned_chunk_texels, "sample_lanes": rep.tuned_sample_lanes,
                                     "blocks_per_sm": rep.tuned_blocks_per_sm,
                                     "stack_depth": rep.tuned_stack_depth, "launch_bound_blocks": rep.tuned_min_blocks,
@@ -304,16 +378,32 @@ def main():
                 "ms_validate_sort": e2e_rep.ms_host[0], "ms_bvh_build": e2e_rep.ms_host[1],
                 "ms_flatten_upload": e2e_rep.ms_host[2], "ms_device": e2e_rep.ms_device,
                 "ms_download_serialize": e2e_rep.ms_download},
-        "roofline": {"bound": "hbm", "kernel": "k_trace_batched", "achieved": achieved, "peak": hbm,
-                     "unit": "GB/s", "frac": achieved / hbm, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                     "traffic": traffic, "algorithmic_bytes_per_launch": int(alg_bytes),
+        "roofline": {"bound": "l2", "kernel": "k_trace_batched", "achieved": achieved, "peak": l2_gbs.value,
+                     "unit": "GB/s", "frac": achieved / l2_gbs.value if l2_gbs.value else None,
+                     "peak_source": f"measured in this run: L2 read bandwidth of this GPU, a {L2_PROBE_BYTES >> 20} MiB "
+                                    "buffer streamed 100 times with L1-bypassing loads (dl_probe_read_bandwidth)",
+                     "l1_read_gbs": l1_gbs.value, "hbm_gbs": hbm, "hbm_source": f"{peak_kind} (MEASURED_PEAKS.json)",
+                     "traffic": traffic, "traffic_frac_of_algorithmic": traffic / alg_bytes if traffic else None,
+                     "limiter": "instruction issue (ncu on the quarter-size outdoor case: issue slots 74 % busy, "
+                                "SIMT efficiency 54 %, L2 throughput 3.9 % of peak)",
+                     "algorithmic_bytes_per_launch": int(alg_bytes),
+                     "bytes_per_unit": "64 per node visit + 48 per triangle test + 76 per (pair, texel) item",
                      "node_visits": int(crep.node_visits), "tri_tests": int(crep.tri_tests),
                      "items": int(crep.work_items)},
     }
     if not args.no_cpu_baseline and world == 1:  # the CPU baseline: rank 0 of a 1-GPU run
-        cb = cpu_baseline(args.workload)
+        # the oracle on the full workload, all host cores, once; its words are the GPU's
+        cb = cpu_baseline(args.workload, full=(inp, opts))
         cb.pop("seconds")
+        cpu_scene = cb.pop("scene")
+        cb["words_equal_gpu"] = bool(cpu_scene.words_equal(result)) and cpu_scene.stats == result.stats
         line["cpu_baseline"] = cb
+        # the target's bounce clause on the seeded CPU sample of the workload
+        if args.workload in ("outdoor", "outdoor_small", "room_grid"):
+            line["config"]["precision"] = precision_slice(args.workload, local)
+            p = line["config"]["precision"]
+            line["config"]["bounce_err_vs_fp64_bitexact"] = p["batched"]["bounce_max_rel_err_vs_fp64"]
+            line["config"]["bounce_err_vs_fp64_refined"] = p["refined"]["bounce_max_rel_err_vs_fp64"]
     print(json.dumps(line))
 
 

@@ -190,9 +190,13 @@ def _hex_id(i):
 
 
 def _options_error(o: BakeOptions):
-    """BakeOptions::validate (src/bake/input.rs:336-373) with the library's messages."""
+    """BakeOptions::validate (src/bake/input.rs:336-373) with the library's messages. The float
+    options are checked as the f32 values the library receives (BakeOptions holds f32), so a
+    density that underflows or overflows f32 fails here as it fails there."""
     bad = None
-    if not (math.isfinite(o.pixel_density) and o.pixel_density > 0.0):
+    with np.errstate(over="ignore", under="ignore"):
+        density, spacing = (float(np.float32(v)) for v in (o.pixel_density, o.sky_probe_spacing))
+    if not (math.isfinite(density) and density > 0.0):
         bad = "pixel density must be positive"
     elif o.max_lightmap_size < 2:
         bad = "the maximum shadow map size must be at least 2"
@@ -204,7 +208,7 @@ def _options_error(o: BakeOptions):
         bad = "the sun map resolution must be 1 to 8192"
     elif o.sky_samples == 0:
         bad = "skies need at least one sample"
-    elif not (math.isfinite(o.sky_probe_spacing) and o.sky_probe_spacing > 0.0):
+    elif not (math.isfinite(spacing) and spacing > 0.0):
         bad = "the sky probe spacing must be positive"
     elif o.bounce_compression not in (8, 6, 5, 4):
         bad = "bounce compression must be 8, 6, 5 or 4 bits"
@@ -521,6 +525,8 @@ def load_library(path: str = LIBRARY_PATH):
     lib.dl_filter_bounce_window_noalloc.restype = C.c_int
     lib.dl_filter_bounce_window_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
                                                     C.c_uint32, C.c_uint32, C.c_void_p]
+    lib.dl_probe_read_bandwidth.restype = C.c_int
+    lib.dl_probe_read_bandwidth.argtypes = [C.c_int, C.c_uint32, C.c_uint64, C.c_uint32, P(C.c_double)]
     _LIB = lib
     return lib
 

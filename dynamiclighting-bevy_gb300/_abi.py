@@ -140,7 +140,7 @@ EXPORTS = [
     "dl_baked_scene_free", "dl_default_options", "dl_session_create", "dl_session_run",
     "dl_session_result", "dl_session_report", "dl_session_destroy", "dl_encode_payload",
     "dl_free", "dl_filter_bounce_window_noalloc", "dl_session_bounce_map", "dl_session_encode_payload",
-    "dl_session_occluder_bvh", "dl_release_memory",
+    "dl_session_occluder_bvh", "dl_release_memory", "dl_probe_read_bandwidth",
 ]
 
 STATUS = {0: "ok", 1: "cancelled", 2: "duplicate id", 3: "invalid mesh", 4: "invalid light",

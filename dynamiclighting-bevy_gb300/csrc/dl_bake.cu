@@ -3383,8 +3383,8 @@ extern "C" dl_status dl_filter_bounce_window_noalloc(const float *in_rgb, float 
                                                      uint32_t height, uint32_t x0, uint32_t y0, uint32_t map_size,
                                                      void *stream) {
     using namespace dl;
-    if (!in_rgb || !out_rgb || in_rgb == out_rgb) {
-        g_error = "the input and output windows must be distinct device buffers";
+    if (!in_rgb || !out_rgb) {
+        g_error = "the input and output windows must be device buffers";
         return DL_INVALID_ARGUMENT;
     }
     uint64_t n = (uint64_t)width * height;
@@ -3393,15 +3393,29 @@ extern "C" dl_status dl_filter_bounce_window_noalloc(const float *in_rgb, float 
                   " texels: the non-allocating filter takes 1 to " + std::to_string(kNoallocMaxTexels) + " texels";
         return DL_INVALID_ARGUMENT;
     }
+    {
+        // the output is written while the input is still read: the two byte ranges must not meet
+        const uintptr_t a = reinterpret_cast<uintptr_t>(in_rgb), b = reinterpret_cast<uintptr_t>(out_rgb);
+        const uintptr_t bytes = (uintptr_t)(n * 3 * sizeof(float));
+        if (a < b + bytes && b < a + bytes) {
+            g_error = "the input and output windows overlap; they must be distinct device buffers";
+            return DL_INVALID_ARGUMENT;
+        }
+    }
     if ((uint64_t)x0 + width > map_size || (uint64_t)y0 + height > map_size) {
         g_error = "the window does not lie inside the map";
         return DL_INVALID_ARGUMENT;
     }
     int device = 0;
     cudaError_t e = cudaGetDevice(&device);
-    if (e != cudaSuccess || device < 0 || device >= kNoallocDevices) {
+    if (e != cudaSuccess) {
         g_error = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
         return DL_CUDA_ERROR;
+    }
+    if (device < 0 || device >= kNoallocDevices) {
+        g_error = "the non-allocating filter runs on devices 0 to " + std::to_string(kNoallocDevices - 1) +
+                  ", the current device is " + std::to_string(device);
+        return DL_UNSUPPORTED;
     }
     float *scratch = nullptr;
     {
@@ -3431,4 +3445,113 @@ extern "C" dl_status dl_filter_bounce_window_noalloc(const float *in_rgb, float 
         return DL_CUDA_ERROR;
     }
     return DL_OK;
+}
+
+// ================================ cache read bandwidth =================================
+// No counterpart in the reference. The roofline of the traversal kernels: their node and
+// triangle reads come from the L1 and L2 caches (the scene's BVH fits in L2), so their bound is
+// the read bandwidth of those caches, which this measures with a plain streaming read.
+
+namespace dl {
+namespace {
+
+// Each thread reads four float4 per iteration (independent loads in flight). Level 2: the
+// blocks stream the whole buffer with L1-bypassing loads (ld.global.cg), `passes` times, so
+// every byte comes from L2 (for a buffer that fits in it). Level 1: each block re-reads its own `slice` float4s with cached
+// loads (ld.global.nc), so after the first pass every byte comes from its SM's L1.
+__global__ void __launch_bounds__(256) k_probe_read(const float4 *__restrict__ buf, uint64_t n4, uint32_t passes,
+                                                    uint32_t level, uint64_t slice, float *sink) {
+    float acc = 0.0f;
+    const float4 *base = buf;
+    uint64_t count = n4, first = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, stride =
+        (uint64_t)gridDim.x * blockDim.x;
+    if (level == 1) {
+        base = buf + ((uint64_t)blockIdx.x * slice) % (n4 - slice + 1);
+        count = slice;
+        first = threadIdx.x;
+        stride = blockDim.x;
+    }
+    for (uint32_t p = 0; p < passes; ++p) {
+        uint64_t i = first;
+        for (; i + 3 * stride < count; i += 4 * stride) {
+            float4 a, b, c, d;
+            if (level == 1) {
+                a = __ldg(base + i);
+                b = __ldg(base + i + stride);
+                c = __ldg(base + i + 2 * stride);
+                d = __ldg(base + i + 3 * stride);
+            } else {
+                a = __ldcg(base + i);
+                b = __ldcg(base + i + stride);
+                c = __ldcg(base + i + 2 * stride);
+                d = __ldcg(base + i + 3 * stride);
+            }
+            acc += (a.x + b.y) + (c.z + d.w);
+        }
+        for (; i < count; i += stride) {
+            float4 a = level == 1 ? __ldg(base + i) : __ldcg(base + i);
+            acc += a.x;
+        }
+    }
+    if (acc == -1.0f) sink[0] = acc;  // never true for the zero buffer; keeps the loads
+}
+
+}  // namespace
+}  // namespace dl
+
+extern "C" dl_status dl_probe_read_bandwidth(int device, uint32_t level, uint64_t bytes, uint32_t passes,
+                                             double *gbs) {
+    using namespace dl;
+    if (!gbs || (level != 1 && level != 2) || passes == 0 || bytes < (1u << 20) || bytes > (1ull << 32)) {
+        g_error = "dl_probe_read_bandwidth: level 1 or 2, 1 MiB to 4 GiB and at least one pass";
+        return DL_INVALID_ARGUMENT;
+    }
+    *gbs = 0.0;
+    int previous = 0;
+    cudaError_t e = cudaGetDevice(&previous);
+    if (e == cudaSuccess) e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        g_error = std::string("dl_probe_read_bandwidth: cudaSetDevice: ") + cudaGetErrorString(e);
+        return DL_CUDA_ERROR;
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    float4 *buf = nullptr;
+    float *sink = nullptr;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    dl_status st = DL_OK;
+    const uint64_t n4 = bytes / sizeof(float4);
+    const uint64_t slice = 32 * 1024 / sizeof(float4);  // level 1: 32 KiB per block, 4 blocks per SM
+    const unsigned blocks = (unsigned)std::max(1, sms) * 4;
+    double best = 0.0;
+    e = cudaMalloc(&buf, n4 * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(&sink, sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(buf, 0, n4 * sizeof(float4));
+    if (e == cudaSuccess) e = cudaEventCreate(&t0);
+    if (e == cudaSuccess) e = cudaEventCreate(&t1);
+    for (int rep = 0; e == cudaSuccess && rep < 6; ++rep) {
+        // the first run is a warm-up: it brings the buffer into L2 (and the slices into L1)
+        cudaEventRecord(t0, 0);
+        k_probe_read<<<blocks, 256>>>(buf, n4, passes, level, slice, sink);
+        cudaEventRecord(t1, 0);
+        e = cudaEventSynchronize(t1);
+        if (e != cudaSuccess) break;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, t0, t1);
+        const double read = level == 1 ? (double)blocks * slice * sizeof(float4) * passes
+                                       : (double)n4 * sizeof(float4) * passes;
+        if (rep > 0 && ms > 0.0f) best = std::max(best, read / (ms * 1e-3) / 1e9);
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        g_error = std::string("dl_probe_read_bandwidth: ") + cudaGetErrorString(e);
+        st = e == cudaErrorMemoryAllocation ? DL_OUT_OF_MEMORY : DL_CUDA_ERROR;
+    }
+    if (t0) cudaEventDestroy(t0);
+    if (t1) cudaEventDestroy(t1);
+    if (buf) cudaFree(buf);
+    if (sink) cudaFree(sink);
+    cudaSetDevice(previous);
+    *gbs = best;
+    return st;
 }

@@ -488,27 +488,29 @@ __device__ __forceinline__ Photon make_photon(const DevScene &sc, const DevLight
     return p;
 }
 
-// Spherical interpolation with linearly interpolated length (glam Vec3::slerp's structure,
-// restated from the standard formula: sin-weighted blend over the angle acos(a.b / |a||b|); a
-// plain lerp when nearly parallel, a half turn about an orthogonal axis when nearly opposite).
-__device__ __forceinline__ float lerpf(float a, float b, float s) { return a + (b - a) * s; }
+// glam's Vec3::slerp as gather_triangle calls it (bounce.rs:270), operation for operation in
+// f32 with no fused operations: the angle from acos_approx (the 7-degree polynomial of
+// Abramowitz & Stegun 4.4.46 in Horner form, sqrt(1 - |x|) * p(|x|), pi minus it below zero), a
+// sine-weighted blend while |cos| < 1 - 3 * 2^-23 with the length interpolated linearly, a turn
+// by pi * s about a unit vector orthogonal to `a` when nearly opposite (Quat::from_axis_angle,
+// then glam's Quat * Vec3), and the plain lerp when nearly equal.
 __device__ __forceinline__ f3 slerp3(f3 a, f3 b, float s) {
-    float la = length(a), lb = length(b);
-    float d = dot(a, b) / (la * lb);
-    if (fabsf(d) < 1.0f - 3e-7f) {
-        float theta = acos_f(d);
-        float sin_theta = sin_f(theta);
-        float t1 = sin_f(theta * (1.0f - s));
-        float t2 = sin_f(theta * s);
-        float rl = lerpf(la, lb, s);
-        return scale(add(scale(scale(a, rl / la), t1), scale(scale(b, rl / lb), t2)), 1.0f / sin_theta);
+    const float la = length(a), lb = length(b);
+    const float d = dot(a, b) / (la * lb);
+    const float eps = 1.1920928955078125e-7f;  // f32::EPSILON
+    if (fabsf(d) < 1.0f - 3.0f * eps) {
+        const float angle = acos_approx(d);
+        const float angle_sin = sin_f(angle);
+        const float t1 = sin_f(angle * (1.0f - s)) / angle_sin;
+        const float t2 = sin_f(angle * s) / angle_sin * (la / lb);
+        return scale(add(scale(a, t1), scale(b, t2)), 1.0f + s * (lb / la - 1.0f));
     }
     if (d < 0.0f) {
-        f3 axis = normalize(fabsf(a.x) > fabsf(a.y) ? f3{-a.z, 0.0f, a.x} : f3{0.0f, a.z, -a.y});
-        float sp, cp;
-        sincos_f(kPiF * s, sp, cp);
-        f3 turned = add(scale(a, cp), scale(cross(axis, a), sp));
-        return scale(turned, lerpf(la, lb, s) / la);
+        const f3 axis = normalize(fabsf(a.x) > fabsf(a.y) ? f3{-a.z, 0.0f, a.x} : f3{0.0f, a.z, -a.y});
+        float sh, ch;
+        sincos_f(kPiF * s * 0.5f, sh, ch);
+        const float q[4] = {axis.x * sh, axis.y * sh, axis.z * sh, ch};
+        return scale(quat_rotate(q, a), 1.0f + s * (lb / la - 1.0f));
     }
     return add(scale(a, 1.0f - s), scale(b, s));
 }

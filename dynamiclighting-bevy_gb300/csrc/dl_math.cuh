@@ -8,9 +8,10 @@
 //   normalize(v) = v * (1 / sqrt(dot(v, v)))
 // Transcendentals of f32 arguments: the binary64 evaluation (Cody–Waite reduction by pi/2 and
 // Taylor series, rounded once) is the definition host and device share. On the device, sin/cos
-// and acos first run in double-float binary32 arithmetic (error-free sums and products, Dekker
-// 1971) to about 2^-40 and keep that result only when Ziv's rounding test shows it rounds to the
-// same binary32 as the exact value; otherwise the binary64 path decides, so both give one answer.
+// first run in double-float binary32 arithmetic (error-free sums and products, Dekker 1971) to
+// about 2^-40 and keep that result only when Ziv's rounding test shows it rounds to the same
+// binary32 as the exact value; otherwise the binary64 path decides, so both give one answer.
+// acos is glam's acos_approx, a binary32 polynomial (below), as the reference's slerp takes it.
 #pragma once
 
 #include <cstdint>
@@ -350,103 +351,26 @@ DL_HD float tan_f(float x) {
     sincos_d((double)x, s, c);
     return (float)(s / c);
 }
-// asin on |y| <= 1/2 by its Maclaurin series, coefficients (2n)!/(4^n (n!)^2 (2n+1)).
-DL_HD double asin_series(double y) {
-    double y2 = y * y;
-    double p = 0.0022014739737101384;
-    p = p * y2 + 0.002338091892111975;
-    p = p * y2 + 0.0024894486782468836;
-    p = p * y2 + 0.00265787063820729;
-    p = p * y2 + 0.002846178401108942;
-    p = p * y2 + 0.0030578216492580306;
-    p = p * y2 + 0.003297059503473485;
-    p = p * y2 + 0.0035692053938259347;
-    p = p * y2 + 0.003880964558837669;
-    p = p * y2 + 0.004240907093679363;
-    p = p * y2 + 0.004660143486915096;
-    p = p * y2 + 0.005153309682319905;
-    p = p * y2 + 0.005740037670841924;
-    p = p * y2 + 0.006447210311889649;
-    p = p * y2 + 0.0073125258735988454;
-    p = p * y2 + 0.008390335809616815;
-    p = p * y2 + 0.009761609529194078;
-    p = p * y2 + 0.011551800896139705;
-    p = p * y2 + 0.01396484375;
-    p = p * y2 + 0.017352764423076924;
-    p = p * y2 + 0.022372159090909092;
-    p = p * y2 + 0.030381944444444444;
-    p = p * y2 + 0.044642857142857144;
-    p = p * y2 + 0.075;
-    p = p * y2 + 0.16666666666666666;
-    p = p * y2 + 1.0;
-    return y * p;
+// glam's acos_approx (the angle of Vec3::slerp): Abramowitz & Stegun 4.4.46 (Hastings'
+// 7-degree polynomial; DirectXMath's XMScalarACos has the same coefficients), in binary32 with
+// no fused operations: sqrt(1 - |x|) * p(|x|) by Horner's rule, and pi minus it for x < 0.
+DL_HD float acos_approx(float v) {
+    const bool nonnegative = v >= 0.0f;
+    const float x = fabsf(v);
+    float omx = 1.0f - x;
+    if (omx < 0.0f) omx = 0.0f;
+    const float root = sqrtf(omx);
+    float r = -0.0012624911f;  // (the library is compiled with --fmad=false: no contraction)
+    r = r * x + 0.0066700901f;
+    r = r * x - 0.0170881256f;
+    r = r * x + 0.0308918810f;
+    r = r * x - 0.0501743046f;
+    r = r * x + 0.0889789874f;
+    r = r * x - 0.2145988016f;
+    r = r * x + 1.5707963050f;
+    r = r * root;
+    return nonnegative ? r : 3.14159265358979323846f - r;
 }
-// acos in binary64: asin's series on |x| <= 1/2, else acos(x) = 2 asin(sqrt((1 - x) / 2)) and
-// pi - 2 asin(sqrt((1 + x) / 2)); rounded once.
-DL_HD float acos_d(float xf) {
-    double x = (double)xf;
-    if (isnan(x) || x > 1.0 || x < -1.0) return NAN;
-    double r;
-    if (fabs(x) <= 0.5)
-        r = (kPio2Hi + kPio2Lo) - asin_series(x);
-    else if (x > 0.0)
-        r = 2.0 * asin_series(sqrt((1.0 - x) * 0.5));
-    else
-        r = kPi - 2.0 * asin_series(sqrt((1.0 + x) * 0.5));
-    return (float)r;
-}
-// The same series in double-float binary32 for |y| <= 1/2: the coefficients of y^3 .. y^13 as
-// binary32 pairs, the tail (y^15 .. y^45, below 2^-17 of the result) in binary32.
-DL_HD FF ff_asin_poly(FF y) {
-    FF z2 = ff_mul(y, y);
-    float z = z2.h;
-    float t = 0.002657870529219508f;
-    t = t * z + 0.0028461783658713102f;
-    t = t * z + 0.0030578216537833214f;
-    t = t * z + 0.003297059563919902f;
-    t = t * z + 0.003569205291569233f;
-    t = t * z + 0.0038809645920991898f;
-    t = t * z + 0.00424090726301074f;
-    t = t * z + 0.00466014351695776f;
-    t = t * z + 0.005153309553861618f;
-    t = t * z + 0.005740037653595209f;
-    t = t * z + 0.006447210442274809f;
-    t = t * z + 0.007312525995075703f;
-    t = t * z + 0.008390335366129875f;
-    t = t * z + 0.009761609137058258f;
-    t = t * z + 0.01155180111527443f;
-    t = t * z + 0.013964843936264515f;
-    FF p = ff_add_f(FF{0.017352763563394547f, 8.596823808382226e-10f}, z * t);
-    p = ff_add(FF{0.022372158244252205f, 8.466569112464128e-10f}, ff_mul(z2, p));
-    p = ff_add(FF{0.0303819440305233f, 4.1392114735749885e-10f}, ff_mul(z2, p));
-    p = ff_add(FF{0.0446428582072258f, -1.0643687042843908e-09f}, ff_mul(z2, p));
-    p = ff_add(FF{0.07500000298023224f, -2.9802322831784522e-09f}, ff_mul(z2, p));
-    p = ff_add(FF{0.1666666716337204f, -4.967053879312289e-09f}, ff_mul(z2, p));
-    return ff_add(y, ff_mul(ff_mul(y, z2), p));
-}
-// acos of a binary32: the double-float path above, kept when Ziv's rounding test proves it
-// correctly rounded, else acos_d (so the value always equals acos_d's).
-DL_HD float acos_f(float x) {
-    if (!(x >= -1.0f && x <= 1.0f)) return NAN;
-    const FF pio2{1.5707963705062866f, -4.371138828673793e-08f}, pi{3.1415927410125732f, -8.742277657347586e-08f};
-    float a = fabsf(x);
-    FF r;
-    if (a <= 0.5f) {
-        r = ff_add(pio2, ff_neg(ff_asin_poly(FF{x, 0.0f})));
-    } else {
-        float t = (1.0f - a) * 0.5f;  // exact: 1 - a by Sterbenz's lemma, then a power of two
-        if (t == 0.0f) return x > 0.0f ? 0.0f : (float)kPi;  // acos_d(1) and acos_d(-1)
-        float sq = sqrtf(t);
-        FF y = ff_fast_sum(sq, fmaf(-sq, sq, t) / (sq + sq));  // sqrt(t) to ~2^-47
-        FF as = ff_asin_poly(y);
-        FF twice{as.h + as.h, as.l + as.l};
-        r = x > 0.0f ? twice : ff_add(pi, ff_neg(twice));
-    }
-    float out;
-    if (ff_rounds_to(r, out)) return out;
-    return acos_d(x);
-}
-
 constexpr float kTau = 6.28318530717958647692f;
 constexpr float kPiF = 3.14159265358979323846f;
 constexpr float kFracPi4 = 0.78539816339744830962f;

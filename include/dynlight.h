@@ -41,7 +41,9 @@ typedef enum dl_status {
     DL_INVALID_OPTIONS = 5, /* BakeError::InvalidOptions (src/bake/input.rs:336-373) */
     DL_CUDA_ERROR = 16,     /* a CUDA call failed; dl_last_error() names it */
     DL_OUT_OF_MEMORY = 17,  /* device or host allocation failed */
-    DL_QUEUE_TIMEOUT = 18,  /* a bounded device wait gave up */
+    DL_QUEUE_TIMEOUT = 18,  /* reserved, never returned: the work queue is claimed with atomic
+                               counters and no kernel of this library waits on another thread,
+                               so there is no device wait to bound */
     DL_BUSY = 19,           /* another bake is running in this process */
     DL_UNSUPPORTED = 20,    /* a scene this library cannot bake (a map side above 65535 texels,
                                an occluder BVH deeper than the traversal stack) */
@@ -381,20 +383,33 @@ void dl_free(void *pointer);
  * thread), this applies the same dilation and 7-tap separable blur to one window of a bounce map
  * held in caller-owned device buffers and allocates nothing.
  *
- * in_rgb / out_rgb: distinct device buffers of width * height RGB float triples, row-major; the
- * window covers map texels [x0, x0 + width) x [y0, y0 + height) of a map_size^2 map (the blur
- * clamps to the map and reads 0 outside the window, as the bake does). At most
- * DL_NOALLOC_MAX_TEXELS texels, else DL_INVALID_ARGUMENT. Runs on the calling thread's current
- * device, enqueued on `stream` (a cudaStream_t, NULL for the legacy default stream).
+ * in_rgb / out_rgb: device buffers of width * height RGB float triples, row-major, whose byte
+ * ranges do not overlap (else DL_INVALID_ARGUMENT); the window covers map texels
+ * [x0, x0 + width) x [y0, y0 + height) of a map_size^2 map (the blur clamps to the map and reads
+ * 0 outside the window, as the bake does). At most DL_NOALLOC_MAX_TEXELS texels, else
+ * DL_INVALID_ARGUMENT; both checks come before any launch. Runs on the calling thread's current
+ * device (devices 0 to 63, else DL_UNSUPPORTED), enqueued on `stream` (a cudaStream_t, NULL for
+ * the legacy default stream).
  *
  * The blur's intermediate lives in one fixed device array of DL_NOALLOC_MAX_TEXELS * 12 bytes
  * (3 MiB) that every device loading the library holds until the process exits. The first call on
- * a device looks up that array's address (cudaGetSymbolAddress); make it before any stream
- * capture. All calls share the array: calls whose work overlaps on the GPU (concurrent streams,
- * threads) race on it, so serialize them. */
+ * a device looks up that array's address (cudaGetSymbolAddress) and keeps it; make that call
+ * before any stream capture. A process that calls cudaDeviceReset on a device must not call this
+ * entry point on that device afterwards: the kept address belongs to the context the reset ended.
+ * All calls share the array: calls whose work overlaps on the GPU (concurrent streams, threads)
+ * race on it, so serialize them. */
 #define DL_NOALLOC_MAX_TEXELS (512u * 512u)
 dl_status dl_filter_bounce_window_noalloc(const float *in_rgb, float *out_rgb, uint32_t width, uint32_t height,
                                           uint32_t x0, uint32_t y0, uint32_t map_size, void *stream);
+
+/* ---- Cache read bandwidth. No counterpart in the reference: a measurement helper for the
+ * roofline of the traversal kernels, whose node and triangle reads are served by the L1 and L2
+ * caches. Reads a zeroed buffer of `bytes` on `device` `passes` times per launch and stores the
+ * best of five timed launches (after one warm-up) in *gbs, in 1e9 bytes per second. level 2:
+ * every block streams the whole buffer with L1-bypassing loads (for a buffer that fits in L2,
+ * the L2 read bandwidth); level 1: each block re-reads its own 32 KiB slice with cached loads
+ * (the L1 read bandwidth). Allocates and frees its buffer; `bytes` from 1 MiB to 4 GiB. */
+dl_status dl_probe_read_bandwidth(int device, uint32_t level, uint64_t bytes, uint32_t passes, double *gbs);
 
 #ifdef __cplusplus
 }

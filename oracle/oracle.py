@@ -31,7 +31,7 @@ def lib():
         _lib.oracle_seed.restype = C.c_uint64
         _lib.oracle_lightmap_size.restype = C.c_uint32
         _lib.oracle_level.restype = C.c_uint8
-        for name in ("oracle_acos", "oracle_tan"):
+        for name in ("oracle_acos_approx", "oracle_tan"):
             getattr(_lib, name).restype = C.c_float
             getattr(_lib, name).argtypes = [C.c_float]
         _lib.oracle_sky_visibility.restype = C.c_float

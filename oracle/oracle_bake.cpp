@@ -1171,7 +1171,7 @@ void oracle_stream_u32(const uint64_t *parts, uint32_t n, uint32_t count, uint32
     for (uint32_t i = 0; i < count; ++i) out[i] = r.next_u32();
 }
 void oracle_sincos(float x, float out[2]) { sincos_f(x, out[0], out[1]); }
-float oracle_acos(float x) { return acos_f(x); }
+float oracle_acos_approx(float x) { return acos_approx(x); }
 float oracle_tan(float x) { return tan_f(x); }
 int oracle_intersect(const float v[9], const float o[3], const float d[3], float max, float *t, float w[3]) {
     V3 vv[3] = {{v[0], v[1], v[2]}, {v[3], v[4], v[5]}, {v[6], v[7], v[8]}};

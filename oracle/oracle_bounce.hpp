@@ -128,31 +128,56 @@ inline PhotonCube build_photon_cube(const Light &light, const Occluders &occ, ui
     return cube;
 }
 
-// ---- slerp (glam Vec3::slerp, restated from the standard formula) ------------------------------
-// Spherical interpolation with linearly interpolated length, for unit-length or near-unit
-// inputs; the near-parallel branches follow glam's structure (lerp when nearly equal, a turn
-// about an orthogonal axis when nearly opposite).
+// ---- slerp (glam 0.33 Vec3::slerp, the reference's bounce.rs:270) ------------------------------
+// glam is not vendored with the reference; its published slerp is restated here:
+//  - the angle comes from glam's acos_approx, not from libm: the 7-degree polynomial of
+//    Abramowitz & Stegun 4.4.46 (Hastings), acos|x| = sqrt(1 - |x|) * p(|x|), evaluated in f32
+//    by Horner's rule with no fused operations, and pi - that for negative x (the form of
+//    DirectXMath's XMScalarACos, which glam follows; the f32 coefficients are the same values);
+//  - the sine-weighted blend is taken when |cos| < 1 - 3 * f32::EPSILON, with the result's
+//    length interpolated linearly between the two lengths;
+//  - nearly opposite vectors turn `a` about a unit vector orthogonal to it by pi * s
+//    (Quat::from_axis_angle, then glam's Quat * Vec3), scaled to the interpolated length;
+//  - nearly equal vectors (or a NaN cosine) take the plain lerp a * (1 - s) + b * s.
+inline float acos_approx(float v) {
+    const bool nonnegative = v >= 0.0f;
+    const float x = std::fabs(v);
+    float omx = 1.0f - x;
+    if (omx < 0.0f) omx = 0.0f;
+    const float root = std::sqrt(omx);
+    float r = -0.0012624911f;
+    r = r * x + 0.0066700901f;
+    r = r * x - 0.0170881256f;
+    r = r * x + 0.0308918810f;
+    r = r * x - 0.0501743046f;
+    r = r * x + 0.0889789874f;
+    r = r * x - 0.2145988016f;
+    r = r * x + 1.5707963050f;
+    r = r * root;
+    return nonnegative ? r : PI_F - r;
+}
 inline V3 any_orthogonal_vector(V3 v) {
     return std::fabs(v.x) > std::fabs(v.y) ? V3{-v.z, 0.0f, v.x} : V3{0.0f, v.z, -v.y};
 }
-inline float lerp_f(float a, float b, float s) { return a + (b - a) * s; }
+constexpr float F32_EPSILON = 1.1920928955078125e-7f;  // f32::EPSILON, 2^-23
 inline V3 slerp(V3 a, V3 b, float s) {
-    float la = length(a), lb = length(b);
-    float d = dot(a, b) / (la * lb);
-    if (std::fabs(d) < 1.0f - 3e-7f) {
-        float theta = acos_f(d);
-        float sin_theta = sin_f(theta);
-        float t1 = sin_f(theta * (1.0f - s));
-        float t2 = sin_f(theta * s);
-        float rl = lerp_f(la, lb, s);
-        return (a * (rl / la) * t1 + b * (rl / lb) * t2) * (1.0f / sin_theta);
+    const float la = length(a), lb = length(b);
+    const float d = dot(a, b) / (la * lb);
+    // the interpolated length as a factor of a's: lerp(|a|, |b|, s) / |a|
+    if (std::fabs(d) < 1.0f - 3.0f * F32_EPSILON) {
+        const float angle = acos_approx(d);
+        const float angle_sin = sin_f(angle);
+        const float t1 = sin_f(angle * (1.0f - s)) / angle_sin;
+        const float t2 = sin_f(angle * s) / angle_sin * (la / lb);
+        return (a * t1 + b * t2) * (1.0f + s * (lb / la - 1.0f));
     }
     if (d < 0.0f) {
-        V3 axis = normalize(any_orthogonal_vector(a));
-        float sp, cp;
-        sincos_f(PI_F * s, sp, cp);
-        V3 turned = a * cp + cross(axis, a) * sp;
-        return turned * (lerp_f(la, lb, s) / la);
+        const V3 axis = normalize(any_orthogonal_vector(a));
+        float sh, ch;
+        sincos_f(PI_F * s * 0.5f, sh, ch);
+        const V3 v = axis * sh;
+        const float q[4] = {v.x, v.y, v.z, ch};
+        return quat_rotate(q, a) * (1.0f + s * (lb / la - 1.0f));
     }
     return a * (1.0f - s) + b * s;
 }

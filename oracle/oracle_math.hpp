@@ -12,12 +12,14 @@
 // normalize(v) = v * (1 / sqrt(dot(v, v))); any_orthonormal_pair is Duff et al. 2017
 // ("Building an Orthonormal Basis, Revisited").
 //
-// Transcendentals (sin, cos, tan, acos, exp of f32 arguments) are evaluated in binary64 and
-// rounded once to binary32: Cody–Waite reduction by pi/2 (Cody & Waite 1980) and the Taylor
-// series of sin/cos (and of asin for acos), so both this oracle and the CUDA kernels produce
-// the correctly rounded f32 in all but ~1e-8 of arguments and agree with each other bit for
-// bit. The reference calls the platform libm (src/bake/mesh_texels.rs:121, random.rs:26,
-// sun.rs:41, light_shape.rs:55, bounce_map.rs:146), whose f32 results are within one ulp.
+// Transcendentals (sin, cos, tan, exp of f32 arguments) are evaluated in binary64 and rounded
+// once to binary32: Cody–Waite reduction by pi/2 (Cody & Waite 1980) and the Taylor series of
+// sin/cos, so both this oracle and the CUDA kernels produce the correctly rounded f32 in all but
+// ~1e-8 of arguments and agree with each other bit for bit. The reference calls the platform
+// libm (src/bake/mesh_texels.rs:121, random.rs:26, sun.rs:41, light_shape.rs:55,
+// bounce_map.rs:146), whose f32 results are within one ulp. Its one arccosine, the angle of
+// glam's slerp (src/bake/bounce.rs:270), is glam's own binary32 polynomial, restated exactly
+// (acos_approx, oracle_bounce.hpp).
 #pragma once
 
 #include <cmath>
@@ -76,7 +78,7 @@ inline V2 vmin2(V2 a, V2 b) { return {fmin_r(a.x, b.x), fmin_r(a.y, b.y)}; }
 inline V2 vmax2(V2 a, V2 b) { return {fmax_r(a.x, b.x), fmax_r(a.y, b.y)}; }
 inline float max_element(V3 a) { return fmax_r(fmax_r(a.x, a.y), a.z); }
 inline V3 vabs(V3 a) { return {std::fabs(a.x), std::fabs(a.y), std::fabs(a.z)}; }
-// geometry.rs:389-391
+// geometry.rs:138-140
 inline bool approx_eq(V3 a, V3 b, float eps) { return max_element(vabs(a - b)) < eps; }
 inline bool v3_finite(V3 a) { return std::isfinite(a.x) && std::isfinite(a.y) && std::isfinite(a.z); }
 
@@ -193,29 +195,6 @@ inline float tan_f(float x) {
     return (float)(s / c);
 }
 
-// asin(y) for |y| <= 1/2 by its Maclaurin series, coefficients (2n)!/(4^n (n!)^2 (2n+1)).
-inline double asin_series(double y) {
-    static const double C[26] = {
-        1.0, 0.16666666666666666, 0.075, 0.044642857142857144, 0.030381944444444444,
-        0.022372159090909092, 0.017352764423076924, 0.01396484375, 0.011551800896139705,
-        0.009761609529194078, 0.008390335809616815, 0.0073125258735988454, 0.006447210311889649,
-        0.005740037670841924, 0.005153309682319905, 0.004660143486915096, 0.004240907093679363,
-        0.003880964558837669, 0.0035692053938259347, 0.003297059503473485, 0.0030578216492580306,
-        0.002846178401108942, 0.00265787063820729, 0.0024894486782468836, 0.002338091892111975,
-        0.0022014739737101384};
-    double y2 = y * y;
-    double p = C[25];
-    for (int n = 24; n >= 0; --n) p = p * y2 + C[n];
-    return y * p;
-}
-// acos by acos(x) = pi/2 - asin(x) for |x| <= 1/2, else 2 asin(sqrt((1 -/+ x)/2)).
-inline double acos_d(double x) {
-    if (std::isnan(x) || x > 1.0 || x < -1.0) return NAN;
-    if (std::fabs(x) <= 0.5) return (PIO2_HI + PIO2_LO) - asin_series(x);
-    if (x > 0.0) return 2.0 * asin_series(std::sqrt((1.0 - x) * 0.5));
-    return PI_D - 2.0 * asin_series(std::sqrt((1.0 + x) * 0.5));
-}
-inline float acos_f(float x) { return (float)acos_d((double)x); }
 inline float exp_f(float x) { return (float)std::exp((double)x); }
 
 constexpr float TAU_F = 6.28318530717958647692f;    // f32 TAU

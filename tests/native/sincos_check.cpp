@@ -1,5 +1,5 @@
-// Compares the library's sin/cos, sin alone and acos (binary32 double-float paths + rounding
-// test, falling back to binary64) with the binary64 paths alone over many arguments; prints
+// Compares the library's sin/cos and sin alone (binary32 double-float paths + rounding test,
+// falling back to binary64) with the binary64 paths alone over many arguments; prints
 // mismatches and the share of arguments that needed the binary64 path. Built and run by tests/test_math_paths.py.
 #include <cstdio>
 #include <cstdlib>
@@ -51,49 +51,5 @@ int main(int argc, char **argv) {
     }
     std::printf("checked %llu mismatches %llu binary64_fallbacks %llu\n", n, mismatch, fallback);
 
-    // acos: the double-float path against acos_d over [-1, 1]: uniform arguments, arguments near
-    // -1, -1/2, 1/2 and 1, and arbitrary bit patterns of magnitude below 1
-    unsigned long long amismatch = 0, afallback = 0;
-    for (unsigned long long i = 0; i < n; ++i) {
-        state = dl::splitmix64(state);
-        double u = (state >> 11) * (1.0 / 9007199254740992.0);
-        float x;
-        switch (i % 4) {
-            case 0: x = (float)(u * 2.0 - 1.0); break;
-            case 1: {
-                const float centers[4] = {-1.0f, -0.5f, 0.5f, 1.0f};
-                x = centers[(state >> 3) & 3] + (float)((u - 0.5) * 1e-3);
-                if (x > 1.0f) x = 1.0f;
-                if (x < -1.0f) x = -1.0f;
-                break;
-            }
-            case 2: x = 1.0f - (float)(u * u * u * 1e-2); break;
-            default: {
-                uint32_t bits = ((uint32_t)(state >> 32) & 0x3F7FFFFFu) | ((uint32_t)(state & 1u) << 31);
-                std::memcpy(&x, &bits, 4);
-            }
-        }
-        float fast = dl::acos_f(x), ref = dl::acos_d(x);
-        if (std::memcmp(&fast, &ref, 4)) {
-            if (amismatch < 10) std::printf("acos mismatch x=%a fast=%a b64=%a\n", x, fast, ref);
-            ++amismatch;
-        }
-        // count fallbacks by re-running the double-float evaluation and its test
-        float a = fabsf(x), t = (1.0f - a) * 0.5f, out;
-        dl::FF r;
-        if (a <= 0.5f) {
-            r = dl::ff_add(dl::FF{1.5707963705062866f, -4.371138828673793e-08f},
-                           dl::ff_neg(dl::ff_asin_poly(dl::FF{x, 0.0f})));
-        } else if (t == 0.0f) {
-            continue;  // +-1: exact constants
-        } else {
-            float sq = sqrtf(t);
-            dl::FF as = dl::ff_asin_poly(dl::ff_fast_sum(sq, fmaf(-sq, sq, t) / (sq + sq)));
-            dl::FF twice{as.h + as.h, as.l + as.l};
-            r = x > 0.0f ? twice : dl::ff_add(dl::FF{3.1415927410125732f, -8.742277657347586e-08f}, dl::ff_neg(twice));
-        }
-        if (!dl::ff_rounds_to(r, out)) ++afallback;
-    }
-    std::printf("acos checked %llu mismatches %llu binary64_fallbacks %llu\n", n, amismatch, afallback);
-    return mismatch || amismatch ? 1 : 0;
+    return mismatch ? 1 : 0;
 }

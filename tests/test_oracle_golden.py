@@ -98,7 +98,7 @@ def test_the_world_origin_is_a_valid_texel_and_opposing_normals_fall_back():
 
 
 def test_burial_rays_cover_the_hemisphere():
-    # src/bake/mesh_texels.rs:389-420
+    # src/bake/mesh_texels.rs:169-200
     seen = []
 
     @orc.DIR_FN
@@ -153,7 +153,7 @@ def test_bit_grids_are_lsb_first_row_major():
 
 
 def test_levels_pack_eight_per_word_and_round():
-    # src/bake/shadow_grid.rs:348-392
+    # src/bake/shadow_grid.rs:184-193, 221-229
     g = np.zeros((3, 3), np.uint8)
     g[0, 0], g[0, 1], g[2, 2] = 15, 1, 7
     assert pack(g, 3, 3, 4) == [0x1F, 7]
@@ -169,7 +169,7 @@ def pad(levels, rect, bits, visited):
 
 
 def test_seam_padding():
-    # src/bake/seams.rs:543-597
+    # src/bake/seams.rs:134-189
     vis = np.zeros((1, 6), np.uint8)
     vis[0, 2] = 1
     out = pad(vis.copy(), (0, 0, 5, 0), 1, vis)
@@ -201,7 +201,7 @@ def dilate(levels, bits):
 
 
 def test_dilation():
-    # src/bake/seams.rs:599-640
+    # src/bake/seams.rs:190-231
     g = np.zeros((7, 7), np.uint8)
     g[2, 2] = 1
     g = dilate(g, 1)
@@ -236,7 +236,7 @@ NONE = 0xFFFFFFFF
 
 
 def test_triangle_words_layout():
-    # src/bake/triangle_words.rs:309-367
+    # src/bake/triangle_words.rs:104-162
     words = serialize([[4, 6, 8, 9], [0, 1, 2, 2]], [2, 0], [[3, 2, NONE], [7, 1, NONE]],
                       [0xAAAA, 0x1, 0xFF], 0)
     M = 0xFFFFFFFF
@@ -254,7 +254,7 @@ def spread(i, o, rect):
 
 
 def test_spread_strips_and_cells():
-    # src/bake/spread.rs:372-407
+    # src/bake/spread.rs:73-108
     for count in [1, 2, 4, 16, 64]:
         for axis, rect in [(0, 1), (1, 1), (0, 0)]:
             strips = sorted(int(spread(i, (0, 0), rect)[axis] * count) for i in range(count))
@@ -276,7 +276,7 @@ def disk(sx, sy):
 
 
 def test_concentric_disk():
-    # src/bake/spread.rs:409-426
+    # src/bake/spread.rs:110-127
     assert np.array_equal(disk(0.5, 0.5), [0, 0])
     for c in [(0, 0), (1, 0), (0, 1), (1, 1)]:
         assert abs(np.linalg.norm(disk(*c)) - 1) < 1e-6
@@ -293,7 +293,7 @@ def cosdir(n, s):
 
 
 def test_cosine_directions_follow_the_cosine():
-    # src/bake/sky.rs:199-213
+    # src/bake/sky.rs:55-70
     n = np.float32([0.3, 0.8, -0.5])
     n = n / np.linalg.norm(n)
     total = 0.0
@@ -411,7 +411,7 @@ def sky_vis(normal, samples, blocked):
 
 
 def test_sky_fractions():
-    # src/bake/sky.rs:215-229
+    # src/bake/sky.rs:71-85
     assert sky_vis((0, 1, 0), 64, lambda d: False) == 1.0
     assert sky_vis((0, 1, 0), 64, lambda d: True) == 0.0
     assert abs(sky_vis((0, 1, 0), 64, lambda d: d[0] < 0) - 0.5) < 0.04
@@ -446,7 +446,7 @@ def pack_bounce(values, bits, rgb=False):
 
 
 def test_bounce_packing_words():
-    # src/bake/bounce_pack.rs:411-478
+    # src/bake/bounce_pack.rs:129-212
     assert [len(pack_bounce([1.0] * 9, b)) for b in (8, 6, 5, 4)] == [3, 2, 2, 2]
     assert pack_bounce([1.0, 0.0, 1.0], 8) == [0x00FF00FF]
     assert pack_bounce([1.0] * 5, 6) == [(1 << 30) - 1]
@@ -603,8 +603,36 @@ def test_transcendentals_are_correctly_rounded():
         L.oracle_sincos(C.c_float(x), out)
         bad += out[0] != np.float32(math.sin(float(x))) or out[1] != np.float32(math.cos(float(x)))
     assert bad == 0
-    for x in np.linspace(-1, 1, 2001).astype(np.float32):
-        assert L.oracle_acos(C.c_float(x)) == np.float32(math.acos(float(x)))
+
+
+def acos_approx_f32(v):
+    """glam's acos_approx restated in numpy binary32 (every operation rounds once): Abramowitz &
+    Stegun 4.4.46, sqrt(1 - |x|) * p(|x|) by Horner's rule, pi minus it below zero."""
+    f = np.float32
+    v = np.asarray(v, np.float32)
+    x = np.abs(v)
+    omx = np.maximum(f(1) - x, f(0))
+    r = np.full_like(x, f(-0.0012624911))
+    for c in (0.0066700901, -0.0170881256, 0.0308918810, -0.0501743046, 0.0889789874, -0.2145988016,
+              1.5707963050):
+        r = (r * x).astype(np.float32) + f(c)
+    r = r * np.sqrt(omx)
+    return np.where(v >= 0, r, f(math.pi) - r).astype(np.float32)
+
+
+def test_acos_approx_is_glams_polynomial():
+    """The slerp angle of gather_triangle (src/bake/bounce.rs:270): glam's acos_approx, bit for
+    bit, within its published accuracy of the true arccosine, exact at 1 and -1."""
+    rng = np.random.default_rng(11)
+    xs = np.concatenate([rng.uniform(-1, 1, 20000), np.linspace(-1, 1, 2001), [0.0, -0.0, 1.0, -1.0],
+                         1 - rng.uniform(0, 1e-3, 2000), -1 + rng.uniform(0, 1e-3, 2000)]).astype(np.float32)
+    want = acos_approx_f32(xs)
+    got = np.array([L.oracle_acos_approx(C.c_float(x)) for x in xs], np.float32)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    assert np.abs(got.astype(np.float64) - np.arccos(xs.astype(np.float64))).max() < 1e-6
+    assert L.oracle_acos_approx(C.c_float(1.0)) == 0.0
+    assert L.oracle_acos_approx(C.c_float(-1.0)) == np.float32(math.pi)
+    assert L.oracle_acos_approx(C.c_float(0.0)) == np.float32(1.5707963050)  # not pi/2 rounded
 
 
 def test_slerp_is_unit_and_spans_the_arc():
@@ -614,6 +642,26 @@ def test_slerp_is_unit_and_spans_the_arc():
     assert np.allclose(list(out), [math.sqrt(0.5), math.sqrt(0.5), 0], atol=1e-6)
     L.oracle_slerp(ptr(a), ptr(b), C.c_float(0.0), out)
     assert np.allclose(list(out), [1, 0, 0], atol=1e-6)
+    # lengths interpolate linearly: |slerp(a, 3b, 0.5)| = 2
+    L.oracle_slerp(ptr(a), ptr(f32(0, 3, 0)), C.c_float(0.5), out)
+    assert abs(np.linalg.norm(list(out)) - 2) < 1e-5
+    # nearly equal vectors take the lerp; nearly opposite ones turn about an orthogonal axis
+    L.oracle_slerp(ptr(a), ptr(f32(1, 1e-5, 0)), C.c_float(0.5), out)
+    assert np.allclose(list(out), [1, 0.5e-5, 0], atol=1e-7)
+    for s in (0.25, 0.5, 0.75):
+        L.oracle_slerp(ptr(a), ptr(f32(-1, 0, 0)), C.c_float(s), out)
+        v = np.array(list(out))
+        assert abs(np.linalg.norm(v) - 1) < 1e-6 and abs(math.acos(max(-1.0, min(1.0, v[0]))) - math.pi * s) < 1e-5
+    # the sine-weighted branch for a generic pair equals the closed form within f32 rounding
+    rng = np.random.default_rng(3)
+    for _ in range(200):
+        p, q = rng.normal(size=3), rng.normal(size=3)
+        p, q = p / np.linalg.norm(p), q / np.linalg.norm(q)
+        s = float(rng.uniform(0.1, 1.0))
+        L.oracle_slerp(ptr(f32(*p)), ptr(f32(*q)), C.c_float(s), out)
+        th = math.acos(float(np.clip(np.dot(p, q), -1, 1)))
+        want = (math.sin((1 - s) * th) * p + math.sin(s * th) * q) / math.sin(th)
+        assert np.allclose(list(out), want, atol=2e-5)
 
 
 def test_orthonormal_pair_and_rotation():
@@ -626,7 +674,7 @@ def test_orthonormal_pair_and_rotation():
         assert abs(np.dot(a, b)) < 1e-6
     r = (C.c_float * 3)()
     L.oracle_quat_rotate(ptr(f32(*dl.scenes.rotation_x(-math.pi / 2))), ptr(f32(0, 0, 1)), r)
-    assert np.allclose(list(r), [0, 1, 0], atol=1e-6)  # a sun turned down is above (shape.rs:152-161)
+    assert np.allclose(list(r), [0, 1, 0], atol=1e-6)  # a sun turned down is above (src/light/shape.rs:153-161)
 
 
 def v3(*x):
@@ -708,7 +756,7 @@ def test_area_lights_reach_and_face_with_their_shape():
 
 
 def test_suns_face_by_direction_and_soften_with_their_disk():
-    # src/bake/light_shape.rs:114-131
+    # src/bake/light_shape.rs:114-128
     floor = np.float32([[0, 0, 0], [0, 0, 1], [1, 0, 0]])
     low = OneLight(fx.sun_light(1, (1.0, 0.02, 0.0), 0.0))
     assert low.bits() == 1, "no disk, hard shadows"

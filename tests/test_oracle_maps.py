@@ -120,7 +120,7 @@ def test_sun_maps_cover_the_scene_across_slanted_rays():
 
 
 def test_empty_scenes_give_a_sun_map_nothing_is_behind():
-    # sun_map.rs:256-268
+    # sun_map.rs:244-254
     sun = dl.BakeLight(id=9, position=(0.0, 0.0, 0.0), radius=1.0,
                        shape=dl.LightShape.sun(scenes.rotation_x(-1.0), 0.53))
     scene = bake([], [sun], sun_map_resolution=256)
@@ -150,7 +150,7 @@ def test_probe_grids_cover_the_bounds_and_stay_within_the_cap():
 
 
 def test_inside_probes_take_their_neighbours_values():
-    # sky_probes.rs:216-231
+    # sky_probes.rs:215-229
     counts = np.array([4, 1, 1], np.uint32)
     values = np.array([[0.5] * 6, [0] * 6, [0] * 6, [1.0] * 6], np.float32)
     valid = np.array([1, 0, 0, 1], np.uint8)

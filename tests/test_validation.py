@@ -81,7 +81,10 @@ def test_light_rules(change, message):
 OPTION_FAULTS = [("pixel_density", -1.0), ("pixel_density", float("nan")), ("max_lightmap_size", 1),
                  ("photon_cube_resolution", 0), ("area_light_samples", 0), ("sun_map_resolution", 0),
                  ("sun_map_resolution", 8193), ("sky_samples", 0), ("sky_probe_spacing", 0.0),
-                 ("sky_probe_spacing", float("inf")), ("bounce_compression", 7)]
+                 ("sky_probe_spacing", float("inf")), ("bounce_compression", 7),
+                 # f32 values: a density that underflows to 0 or overflows to infinity as the f32
+                 # BakeOptions holds (src/bake/input.rs:136-164), likewise the probe spacing
+                 ("pixel_density", 1e-50), ("pixel_density", 1e50), ("sky_probe_spacing", 1e-60)]
 
 
 @pytest.mark.parametrize("name, value", OPTION_FAULTS)
@@ -90,6 +93,16 @@ def test_option_rules_and_the_mirrors_copy_agree(name, value):
     opts = dataclasses.replace(opts, **{name: value})
     text = fails(inp, opts, "InvalidOptions", "invalid bake options: ")
     assert text == "InvalidOptions: " + dl._options_error(opts)
+
+
+def test_f32_rounded_options_come_before_a_length_mismatch():
+    """An f32-underflowing density and a per-vertex array of the wrong length: the mirror checks
+    the options first (src/bake/baker.rs:32-35), as the f32 the library would receive, so it
+    reports InvalidOptions as the reference does, not InvalidMesh."""
+    inp, opts = room()
+    inp.meshes[2].uv1 = inp.meshes[2].uv1[:-1]
+    opts = dataclasses.replace(opts, pixel_density=1e-50)
+    fails(inp, opts, "InvalidOptions", "pixel density must be positive")
 
 
 def test_valid_options_pass_the_mirrors_copy():

@@ -17,7 +17,8 @@ from dynlight_gb300 import scenes
 from oracle import oracle
 from oracle.oracle import f32, ptr
 
-pytestmark = pytest.mark.gpu
+MAX_TEXELS = 512 * 512  # DL_NOALLOC_MAX_TEXELS
+INVALID_ARGUMENT = 21
 
 
 def bounce_scene():
@@ -65,6 +66,7 @@ def stored_bytes(words, offset, count):
     return [(int(words[offset + i // 4]) >> (8 * (i % 4))) & 0xFF for i in range(count)]
 
 
+@pytest.mark.gpu
 def test_noalloc_filter_matches_the_bake_twice_in_a_row():
     torch = pytest.importorskip("torch")
     lib = dl.load_library()
@@ -116,9 +118,70 @@ def test_noalloc_filter_matches_the_bake_twice_in_a_row():
     assert np.array_equal(outputs[0], outputs[1])
 
 
-def test_noalloc_filter_rejects_windows_beyond_its_limit():
+@pytest.mark.gpu
+def test_noalloc_filter_takes_a_window_of_exactly_its_limit():
+    """A 512 x 512 window (DL_NOALLOC_MAX_TEXELS texels) is accepted and filtered as the oracle's
+    BounceMap filters the same window (dilation and blur of bounce_map.rs:67-112)."""
+    torch = pytest.importorskip("torch")
     lib = dl.load_library()
-    side = 513  # 513^2 > DL_NOALLOC_MAX_TEXELS
-    status = lib.dl_filter_bounce_window_noalloc(C.c_void_p(16), C.c_void_p(32), side, side, 0, 0, 1024, None)
-    assert status == 21  # DL_INVALID_ARGUMENT
+    size = 512
+    rng = np.random.default_rng(7)
+    n = 3000
+    xs, ys = rng.integers(0, size, n), rng.integers(0, size, n)
+    vals = rng.random((n, 3), dtype=np.float32)
+    tex = np.concatenate([np.stack([xs, ys], 1).astype(np.float32), vals], 1).astype(np.float32)
+    want = np.zeros(size * size * 3, np.float32)
+    win = (C.c_uint32 * 4)()
+    oracle.lib().oracle_bounce_map(size, (C.c_uint32 * 4)(4, 4, size - 5, size - 5), ptr(np.ascontiguousarray(tex)),
+                                   n, ptr(want), win)
+    assert list(win) == [0, 0, size - 1, size - 1]
+    pre = np.zeros((size, size, 3), np.float32)
+    for (x, y), v in zip(zip(xs, ys), vals):  # later texels overwrite earlier ones, as BounceMap::set
+        pre[y, x] = v
+    dev = torch.device("cuda:0")
+    src = torch.from_numpy(pre.reshape(-1)).to(dev)
+    out = torch.full((size * size * 3,), float("nan"), dtype=torch.float32, device=dev)
+    status = lib.dl_filter_bounce_window_noalloc(C.c_void_p(src.data_ptr()), C.c_void_p(out.data_ptr()), size, size,
+                                                 0, 0, size, None)
+    assert status == 0, lib.dl_last_error()
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), want)
+
+
+@pytest.mark.gpu
+def test_noalloc_filter_rejects_one_texel_beyond_its_limit_without_launching():
+    """A 1 x (DL_NOALLOC_MAX_TEXELS + 1) window in real device buffers of that size is rejected
+    before any launch: the output keeps its sentinel."""
+    torch = pytest.importorskip("torch")
+    lib = dl.load_library()
+    n = MAX_TEXELS + 1
+    dev = torch.device("cuda:0")
+    src = torch.zeros(n * 3, dtype=torch.float32, device=dev)
+    out = torch.full((n * 3,), float("nan"), dtype=torch.float32, device=dev)
+    status = lib.dl_filter_bounce_window_noalloc(C.c_void_p(src.data_ptr()), C.c_void_p(out.data_ptr()), 1, n,
+                                                 0, 0, n, None)
+    assert status == INVALID_ARGUMENT
     assert b"texels" in lib.dl_last_error()
+    torch.cuda.synchronize()
+    assert bool(torch.isnan(out).all())
+
+
+def test_noalloc_filter_checks_its_arguments_before_any_cuda_call():
+    """Size, map and overlap checks return before the library touches CUDA (so they run on a
+    host without a GPU): over the limit in either shape, windows outside the map, and input and
+    output ranges that overlap by any amount."""
+    lib = dl.load_library()
+    f = lib.dl_filter_bounce_window_noalloc
+    a, b = 1 << 20, 1 << 24  # never dereferenced: every call below is rejected on the host
+    assert f(C.c_void_p(a), C.c_void_p(b), 513, 513, 0, 0, 1024, None) == INVALID_ARGUMENT
+    assert f(C.c_void_p(a), C.c_void_p(b), 512, 513, 0, 0, 1024, None) == INVALID_ARGUMENT
+    assert f(C.c_void_p(a), C.c_void_p(b), 1, MAX_TEXELS + 1, 0, 0, MAX_TEXELS + 1, None) == INVALID_ARGUMENT
+    assert b"texels" in lib.dl_last_error()
+    assert f(C.c_void_p(a), C.c_void_p(b), 0, 4, 0, 0, 16, None) == INVALID_ARGUMENT
+    assert f(C.c_void_p(a), C.c_void_p(b), 8, 8, 9, 0, 16, None) == INVALID_ARGUMENT
+    assert b"inside the map" in lib.dl_last_error()
+    window = 8 * 8 * 3 * 4  # bytes of an 8 x 8 window
+    for shift in (0, 4, window - 4, -(window - 4)):
+        assert f(C.c_void_p(a), C.c_void_p(a + shift), 8, 8, 0, 0, 16, None) == INVALID_ARGUMENT, shift
+        assert b"overlap" in lib.dl_last_error()
+    assert f(None, C.c_void_p(b), 8, 8, 0, 0, 16, None) == INVALID_ARGUMENT
