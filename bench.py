@@ -350,7 +350,7 @@ def main():
     if rank != 0:
         return
     line = {
-        "metric": "shadow rays/s (bake of the workload, device-resident)",
+        "metric": METRIC,
         "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded generator)",

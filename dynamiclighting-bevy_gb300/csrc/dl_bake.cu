@@ -577,12 +577,15 @@ struct BounceArgs {
 // shift-aligned coherent order instead (shifted_sample): round r of every group in the warp
 // traces ranks r * lanes + k, so the warp's texels (neighbours along a triangle) send their rays
 // in about the same directions. A sample whose closest hit faces the sun and is lit by it
-// stores its value and its shadow ray's origin in the group's scratch (global memory, indexed
-// by sample) and sets its bit in the group's mask (shared memory); after the closest-hit rounds
-// the group traces those shadow rays together, W at a time (parallel rays towards the sun),
-// clearing the bits of blocked ones, and the leader adds the values left in the mask in sample
-// order. Dynamic shared memory holds the traversal stacks, one float4 contribution slot per
-// thread and the groups' masks. MINB is the launch bound's blocks per SM (the register budget: 6 leaves the compiler its 80 registers, 8 asks for 64).
+// stores its value, its index and its shadow ray's origin in the next free slot of the group's
+// scratch (global memory; slots are taken in arrival order, so a group touches only as many as
+// it holds, a few lines that stay in L2) and sets its bit in the group's mask (shared memory).
+// After the closest-hit rounds the group traces the held shadow rays together, W at a time
+// (parallel rays towards the sun), marking blocked ones in a second mask; each open sample's
+// value then moves to its rank among the open samples (popcounts of the masks), and the group
+// loads those values W at a time while the leader adds them, in sample order, as the reference
+// does (sun_bounce.rs:70). Dynamic shared memory holds the traversal stacks, one float4
+// contribution slot per thread and the groups' masks. MINB is the launch bound's blocks per SM (the register budget: 6 leaves the compiler its 80 registers, 8 asks for 64).
 template <bool REFINE, int MINB>
 __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs a) {
     extern __shared__ int smem[];
@@ -643,21 +646,28 @@ __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs
         const bool aligned = sun && samples >= 32 && samples <= a.buffered && !(samples & (samples - 1));
         const uint32_t shift = aligned ? net_shift(samples, sg.off) : 0u;
         FSum3<REFINE> sum;
+        uint32_t filled = 0;  // aligned sun gathers: scratch slots filled so far (the same in the group)
         const uint32_t rounds = __reduce_max_sync(0xFFFFFFFFu, (samples + W - 1) / W);
         for (uint32_t r = 0; r < rounds; ++r) {
             const uint32_t k = r * W + sub;
             if (aligned) {
+                SunHit h{f3{0.0f, 0.0f, 0.0f}, f3{0.0f, 0.0f, 0.0f}, false};
+                uint32_t i = 0;
                 if (k < samples) {
-                    const uint32_t i = shifted_sample(sc, samples, shift, k);
-                    SunHit h = sun_hit<REFINE>(sc, sc.lights[s], origin, normal, sg, i, my, kBlock, &vis);
+                    i = shifted_sample(sc, samples, shift, k);
+                    h = sun_hit<REFINE>(sc, sc.lights[s], origin, normal, sg, i, my, kBlock, &vis);
                     rays += h.pending ? 2 : 1;
-                    if (h.pending) {
-                        scratch[2 * i] = make_float4(h.value.x, h.value.y, h.value.z, 0.0f);
-                        scratch[2 * i + 1] = make_float4(h.point.x, h.point.y, h.point.z, 0.0f);
-                        atomicOr(&lit[i >> 5], 1u << (i & 31u));
-                    }
                 }
-                continue;  // no per-round sum: the group syncs below use group masks
+                // the group's pending samples of this round take the next slots, in lane order
+                const unsigned mine = __ballot_sync(group_lanes, h.pending);
+                if (h.pending) {
+                    const uint32_t slot = filled + __popc(mine & ((1u << lane) - 1u));
+                    scratch[2 * slot] = make_float4(h.value.x, h.value.y, h.value.z, __uint_as_float(i));
+                    scratch[2 * slot + 1] = make_float4(h.point.x, h.point.y, h.point.z, 0.0f);
+                    atomicOr(&lit[i >> 5], 1u << (i & 31u));
+                }
+                filled += __popc(mine);
+                continue;  // no per-round sum: the phases below add the values in sample order
             }
             Contribution c{f3{0.0f, 0.0f, 0.0f}, false, 0};
             if (k < samples) {
@@ -683,34 +693,47 @@ __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs
         }
         __syncwarp();
         if (aligned) {
-            // the shadow rays of the lit hits, spread over the group's lanes in sample order
-            uint32_t nth = 0;
-            for (uint32_t w = 0; w < samples / 32; ++w) {
-                uint32_t bits = lit[w];  // read-only in this phase
-                while (bits) {
-                    const uint32_t b = __ffs(bits) - 1;
-                    bits &= bits - 1;
-                    if (nth++ % W != sub) continue;
-                    const uint32_t i = w * 32 + b;
-                    const float4 q = scratch[2 * i + 1];
-                    if (!sun_open<REFINE>(sc, sc.lights[s], f3{q.x, q.y, q.z}, my, kBlock, &vis))
-                        atomicOr(&blocked[w], 1u << b);
-                }
+            // the shadow rays of the held samples, slot by slot across the group's lanes
+            for (uint32_t j = sub; j < filled; j += W) {
+                const float4 q = scratch[2 * j + 1];
+                const uint32_t i = __float_as_uint(scratch[2 * j].w);
+                if (!sun_open<REFINE>(sc, sc.lights[s], f3{q.x, q.y, q.z}, my, kBlock, &vis))
+                    atomicOr(&blocked[i >> 5], 1u << (i & 31u));
             }
         }
         __syncwarp();
-        if (aligned && sub == 0) {
-            for (uint32_t w = 0; w < samples / 32; ++w) {
-                uint32_t bits = lit[w] & ~blocked[w];
-                while (bits) {
-                    const uint32_t b = __ffs(bits) - 1;
-                    bits &= bits - 1;
-                    const float4 q = scratch[2 * (w * 32 + b)];
-                    sum.add(f3{q.x, q.y, q.z});
+        uint32_t open_count = 0;
+        if (aligned) {
+            // each open sample's value moves to its rank among the open samples in sample order
+            // (into the shadow-ray origins' half of the slots, which is no longer read)
+            for (uint32_t j = sub; j < filled; j += W) {
+                const float4 v = scratch[2 * j];
+                const uint32_t i = __float_as_uint(v.w), w = i >> 5, b = i & 31u;
+                const uint32_t open = lit[w] & ~blocked[w];
+                if ((open >> b) & 1u) {
+                    uint32_t rank = __popc(open & ((1u << b) - 1u));
+                    for (uint32_t u = 0; u < w; ++u) rank += __popc(lit[u] & ~blocked[u]);
+                    scratch[2 * rank + 1] = v;
                 }
-                lit[w] = 0u;
-                blocked[w] = 0u;
             }
+            for (uint32_t u = 0; u < samples / 32; ++u) open_count += __popc(lit[u] & ~blocked[u]);
+        }
+        __syncwarp();
+        if (aligned) {
+            // the group loads the ordered values W at a time; the leader adds them in order
+            const uint32_t lane0 = lane - sub;
+            for (uint32_t base = 0; base < open_count; base += W) {
+                float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                if (base + sub < open_count) q = scratch[2 * (base + sub) + 1];
+                const uint32_t n = min(W, open_count - base);
+                for (uint32_t t = 0; t < n; ++t) {
+                    const float x = __shfl_sync(group_lanes, q.x, lane0 + t);
+                    const float y = __shfl_sync(group_lanes, q.y, lane0 + t);
+                    const float z = __shfl_sync(group_lanes, q.z, lane0 + t);
+                    if (sub == 0) sum.add(f3{x, y, z});
+                }
+            }
+            for (uint32_t w = sub; w < 2 * words; w += W) lit[w] = 0u;  // lit, then blocked
         }
         __syncwarp();
         if (valid && sub == 0) {
