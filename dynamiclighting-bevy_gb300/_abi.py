@@ -56,7 +56,7 @@ class DlBakeConfig(C.Structure):
                 ("chunk_texels", C.c_uint32), ("sample_lanes", C.c_uint32),
                 ("blocks_per_sm", C.c_uint32), ("count_visits", C.c_uint32),
                 ("refine_epsilon", C.c_float), ("no_autotune", C.c_uint32), ("host_bvh", C.c_uint32),
-                ("reserved", C.c_uint32 * 4)]
+                ("max_device_mib", C.c_uint32), ("reserved", C.c_uint32 * 3)]
 
 
 class DlBakeReport(C.Structure):
@@ -73,7 +73,8 @@ class DlBakeReport(C.Structure):
                 ("tuned_sample_lanes", C.c_uint32), ("tuned_blocks_per_sm", C.c_uint32),
                 ("tuned_stack_depth", C.c_uint32), ("tuned_min_blocks", C.c_uint32),
                 ("tune_trials", C.c_uint32), ("ms_tune", C.c_double),
-                ("tuned_gather_lanes", C.c_uint32), ("reserved_report", C.c_uint32)]
+                ("tuned_gather_lanes", C.c_uint32), ("cancel_stops", C.c_uint32),
+                ("gather_node_visits", C.c_uint64), ("gather_tri_tests", C.c_uint64)]
 
 
 class DlLightBvhNode(C.Structure):

@@ -42,6 +42,7 @@ struct Counters {
     unsigned long long rays, burial_rays, lights_removed, bounce_rays, photon_rays, cancelled;
     unsigned long long node_visits, tri_tests;  // instrumented visibility kernel only
     unsigned long long retests;                 // refined form: binary64 re-tests
+    unsigned long long gather_node_visits, gather_tri_tests;  // instrumented gather kernel only
 };
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
@@ -362,6 +363,19 @@ __device__ __forceinline__ uint32_t pair_of(const TraceArgs &a, unsigned long lo
     return lo;
 }
 
+// Whether a warp's lane 0 should stop claiming work: the cancel flag is read every 16th claim;
+// once it is seen, the warp counts itself in `ctr->cancelled` and every later claim stops too.
+constexpr uint32_t kStopped = 0x80000000u;
+__device__ __forceinline__ bool cancel_seen(const volatile uint32_t *cancel, Counters *ctr, uint32_t &grabs) {
+    if (grabs & kStopped) return true;
+    if ((++grabs & 15u) == 0 && *cancel) {
+        grabs |= kStopped;
+        atomicAdd(&ctr->cancelled, 1ull);
+        return true;
+    }
+    return false;
+}
+
 // Claims the next chunk of a queue phase for the warp: the first item of chunk c is
 // first + c * size * sample_every. Returns `end` when the phase is drained or cancelled.
 __device__ __forceinline__ unsigned long long claim(const TraceArgs &a, unsigned long long *head,
@@ -369,10 +383,13 @@ __device__ __forceinline__ unsigned long long claim(const TraceArgs &a, unsigned
                                                     unsigned long long end, uint32_t &grabs) {
     unsigned long long base = 0;
     if (lane_id() == 0) {
-        unsigned long long c = atomicAdd(head, 1ull);
-        base = first + c * size * a.sample_every;
-        if ((++grabs & 15u) == 0 && *a.cancel) base = end;
-        if (base > end) base = end;
+        if (cancel_seen(a.cancel, a.ctr, grabs)) {
+            base = end;
+        } else {
+            unsigned long long c = atomicAdd(head, 1ull);
+            base = first + c * size * a.sample_every;
+            if (base > end) base = end;
+        }
     }
     return __shfl_sync(0xFFFFFFFFu, base, 0);
 }
@@ -567,6 +584,7 @@ struct BounceArgs {
     uint32_t buffered;      // sun samples a lane group can hold for the aligned order (0: none)
     float4 *scratch;        // per lane group (blockIdx * groups + group): 2 * buffered float4
     unsigned long long *head;  // steps claimed so far (32 / lanes items per step)
+    const volatile uint32_t *cancel;  // the bake's cancel flag, read every 16th claim
 };
 
 // gather_triangle / gather_sun (bounce.rs:235-292, sun_bounce.rs:24-80): a group of `lanes`
@@ -586,7 +604,7 @@ struct BounceArgs {
 // loads those values W at a time while the leader adds them, in sample order, as the reference
 // does (sun_bounce.rs:70). Dynamic shared memory holds the traversal stacks, one float4
 // contribution slot per thread and the groups' masks. MINB is the launch bound's blocks per SM (the register budget: 6 leaves the compiler its 80 registers, 8 asks for 64).
-template <bool REFINE, int MINB>
+template <bool COUNT, bool REFINE, int MINB>
 __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs a) {
     extern __shared__ int smem[];
     int *my = smem + threadIdx.x;
@@ -603,10 +621,12 @@ __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs
     __syncwarp();
     unsigned long long rays = 0;
     Visits vis{0, 0, 0};
+    uint32_t grabs = 0;
     for (;;) {
-        unsigned long long step = 0;
-        if (lane == 0) step = atomicAdd(a.head, 1ull);
+        unsigned long long step = ~0ull;
+        if (lane == 0 && !cancel_seen(a.cancel, a.ctr, grabs)) step = atomicAdd(a.head, 1ull);
         step = __shfl_sync(0xFFFFFFFFu, step, 0);
+        if (step == ~0ull) break;  // cancelled (uniform across the warp)
         unsigned long long base = step * per_step * a.sample_every;
         if (base >= a.items) break;  // uniform across the warp
         unsigned long long item = base + lane / W;
@@ -655,7 +675,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs
                 uint32_t i = 0;
                 if (k < samples) {
                     i = shifted_sample(sc, samples, shift, k);
-                    h = sun_hit<REFINE>(sc, sc.lights[s], origin, normal, sg, i, my, kBlock, &vis);
+                    h = sun_hit<COUNT, REFINE>(sc, sc.lights[s], origin, normal, sg, i, my, kBlock, &vis);
                     rays += h.pending ? 2 : 1;
                 }
                 // the group's pending samples of this round take the next slots, in lane order
@@ -673,9 +693,9 @@ __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs
             if (k < samples) {
                 const DevLight &l = sc.lights[s];
                 if (sun) {
-                    c = sun_sample<REFINE>(sc, l, origin, normal, sg, k, my, kBlock, &vis);
+                    c = sun_sample<COUNT, REFINE>(sc, l, origin, normal, sg, k, my, kBlock, &vis);
                 } else {
-                    Tracer<false, REFINE> tr{sc, origin, (l.flags & kLightAlpha) != 0, my, kBlock, &vis};
+                    Tracer<COUNT, REFINE> tr{sc, origin, (l.flags & kLightAlpha) != 0, my, kBlock, &vis};
                     c = local_sample(sc, l, a.photons + (size_t)l.cube * 6 * a.res * a.res, a.res, normal, lg, k, tr);
                     lg.rng.advance(2ull * (W - 1));  // to the lane's next sample, k + W
                 }
@@ -697,7 +717,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs
             for (uint32_t j = sub; j < filled; j += W) {
                 const float4 q = scratch[2 * j + 1];
                 const uint32_t i = __float_as_uint(scratch[2 * j].w);
-                if (!sun_open<REFINE>(sc, sc.lights[s], f3{q.x, q.y, q.z}, my, kBlock, &vis))
+                if (!sun_open<COUNT, REFINE>(sc, sc.lights[s], f3{q.x, q.y, q.z}, my, kBlock, &vis))
                     atomicOr(&blocked[i >> 5], 1u << (i & 31u));
             }
         }
@@ -744,6 +764,13 @@ __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs
     }
     unsigned long long total = warp_sum(rays);
     if (lane_id() == 0 && total) atomicAdd(&a.ctr->bounce_rays, total);
+    if (COUNT) {
+        unsigned long long n = warp_sum(vis.nodes), t = warp_sum(vis.tris);
+        if (lane_id() == 0) {
+            atomicAdd(&a.ctr->gather_node_visits, n);
+            atomicAdd(&a.ctr->gather_tri_tests, t);
+        }
+    }
     if (REFINE) add_retests(a.ctr, vis.retests);
 }
 
@@ -1497,16 +1524,35 @@ void release_pooled_device_memory() {
         if (cudaDeviceGetDefaultMemPool(&pool, d) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
     }
 }
-void *dev_malloc(size_t bytes, cudaStream_t st) {
+// The device memory a session holds (scene, BVH, its build scratch, every stage's buffers)
+// against the caller's cap (dl_bake_config.max_device_mib; 0: none). An allocation past the cap
+// fails like a failed cudaMallocAsync, so the bake reports DL_OUT_OF_MEMORY.
+struct DeviceBudget {
+    uint64_t cap = 0, held = 0;
+    void reserve(size_t b) {
+        if (cap && held + b > cap)
+            throw CudaError{cudaErrorMemoryAllocation, "device memory cap (dl_bake_config.max_device_mib)"};
+        held += b;
+    }
+    void release(size_t b) { held -= std::min<uint64_t>(held, b); }
+};
+
+void *dev_malloc(size_t bytes, cudaStream_t st, DeviceBudget *budget) {
     void *p = nullptr;
-    CK(cudaMallocAsync(&p, std::max<size_t>(bytes, 16), st));
+    const size_t b = std::max<size_t>(bytes, 16);
+    if (budget) budget->reserve(b);
+    cudaError_t e = cudaMallocAsync(&p, b, st);
+    if (e != cudaSuccess) {
+        if (budget) budget->release(b);
+        throw CudaError{e, "cudaMallocAsync"};
+    }
     return p;
 }
 
 template <class T>
-T *dev_alloc(std::vector<void *> &owned, cudaStream_t st, size_t count, uint64_t &bytes) {
+T *dev_alloc(std::vector<void *> &owned, cudaStream_t st, size_t count, uint64_t &bytes, DeviceBudget *budget) {
     size_t b = std::max<size_t>(count * sizeof(T), 16);
-    void *p = dev_malloc(b, st);
+    void *p = dev_malloc(b, st, budget);
     owned.push_back(p);
     bytes += b;
     return static_cast<T *>(p);
@@ -1523,6 +1569,7 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 struct Pool {
     std::map<std::string, std::pair<void *, size_t>> bufs;
     cudaStream_t stream = nullptr;
+    DeviceBudget *budget = nullptr;
     uint64_t bytes = 0;
     uint64_t generation = 0;  // bumped whenever a buffer moves
     template <class T>
@@ -1533,8 +1580,10 @@ struct Pool {
         if (it != bufs.end()) {
             cudaFreeAsync(it->second.first, stream);
             bytes -= it->second.second;
+            if (budget) budget->release(it->second.second);
+            bufs.erase(it);
         }
-        void *p = dev_malloc(b, stream);
+        void *p = dev_malloc(b, stream, budget);
         bufs[name] = {p, b};
         bytes += b;
         ++generation;
@@ -1542,8 +1591,12 @@ struct Pool {
     }
     // Frees every buffer on the stream; the session calls it before destroying its stream.
     void release() {
-        for (auto &kv : bufs) cudaFreeAsync(kv.second.first, stream);
+        for (auto &kv : bufs) {
+            cudaFreeAsync(kv.second.first, stream);
+            if (budget) budget->release(kv.second.second);
+        }
         bufs.clear();
+        bytes = 0;
     }
 };
 
@@ -1565,6 +1618,7 @@ struct dl_session {
     uint64_t grid_words = 0;
     std::vector<uint32_t> mesh_tri_base;
     Pool pool;
+    DeviceBudget budget;  // device memory held against config.max_device_mib
     Counters *ctr = nullptr;
     uint32_t *cancel_dev = nullptr;
     dl_bake_report report{};
@@ -1637,12 +1691,17 @@ T read_back(dl_session &s, const T *p) {
 }
 unsigned grid_for(size_t n, unsigned block = kBlock) { return (unsigned)std::max<size_t>(1, (n + block - 1) / block); }
 
-// Blocks the caller until the stream drains, forwarding a cancel request to the device flag.
+// Blocks the caller until the stream drains, forwarding a cancel request to the device flag. A
+// forwarded request's copy (on the side stream) is waited for too, so that it cannot land after
+// the next run has cleared the flag.
 void wait(dl_session &s, dl_progress *progress) {
     bool forwarded = false;
     for (;;) {
         cudaError_t q = cudaStreamQuery(s.stream);
-        if (q == cudaSuccess) return;
+        if (q == cudaSuccess) {
+            if (forwarded) CK(cudaStreamSynchronize(s.side));
+            return;
+        }
         if (q != cudaErrorNotReady) throw CudaError{q, "stream"};
         if (progress && progress->cancel && !forwarded) {
             static const uint32_t one = 1;
@@ -1651,6 +1710,16 @@ void wait(dl_session &s, dl_progress *progress) {
         }
         std::this_thread::yield();
     }
+}
+
+// A run that stops on the cancel flag: its report records how many warps of the device work
+// queues saw the flag and stopped claiming work (0 when the request came between stages).
+dl_status cancelled_run(dl_session &s) {
+    Counters c{};
+    CK(cudaMemcpyAsync(&c, s.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s.stream));
+    CK(cudaStreamSynchronize(s.stream));
+    s.report.cancel_stops = (uint32_t)c.cancelled;
+    return DL_CANCELLED;
 }
 
 // `progress`, when given, is checked for cancellation once validation has passed and before the
@@ -1715,6 +1784,8 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     CK(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
     keep_freed_device_memory(s->device);
     s->pool.stream = s->stream;
+    s->budget.cap = (uint64_t)s->config.max_device_mib << 20;
+    s->pool.budget = &s->budget;
 
     // flatten meshes
     uint32_t M = (uint32_t)h.meshes.size();
@@ -1770,7 +1841,7 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     uint64_t &bytes = s->scene_bytes;
     auto up = [&](const void *src, size_t n, auto *&dst) {
         using T = std::remove_const_t<std::remove_pointer_t<std::remove_reference_t<decltype(dst)>>>;
-        T *p = dev_alloc<T>(s->owned, s->stream, n / sizeof(T) + 1, bytes);
+        T *p = dev_alloc<T>(s->owned, s->stream, n / sizeof(T) + 1, bytes, &s->budget);
         if (n) CK(cudaMemcpyAsync(p, src, n, cudaMemcpyHostToDevice, s->stream));
         dst = p;
         s->report.h2d_bytes += n;
@@ -1810,10 +1881,10 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     } else {
         auto t_bvh = std::chrono::steady_clock::now();
         DeviceBvhInput bi{sc.positions, sc.indices, sc.mesh_vertex_base, sc.mesh_index_base, sc.occ_mesh,
-                          sc.occ_tri, N};
+                          sc.occ_tri, N, &s->budget.held, s->budget.cap};
         DeviceBvh db;
         try {
-            build_bvh_device(bi, [&](size_t b) { return (void *)dev_alloc<uint8_t>(s->owned, s->stream, b, bytes); }, s->stream,
+            build_bvh_device(bi, [&](size_t b) { return (void *)dev_alloc<uint8_t>(s->owned, s->stream, b, bytes, &s->budget); }, s->stream,
                              db);
         } catch (const DeviceBvhError &e) {
             throw CudaError{e.code, e.what};
@@ -1833,11 +1904,11 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
         sc.tri_e2 = db.tri_e2;
         sc.occ_leaf = db.occ_leaf;
         if (N == 0) {  // no occluders: small placeholders, which traversal never reads
-            sc.nodes = dev_alloc<float4>(s->owned, s->stream, 4, bytes);
-            sc.tri_v0 = dev_alloc<float4>(s->owned, s->stream, 1, bytes);
-            sc.tri_e1 = dev_alloc<float4>(s->owned, s->stream, 1, bytes);
-            sc.tri_e2 = dev_alloc<float4>(s->owned, s->stream, 1, bytes);
-            sc.occ_leaf = dev_alloc<uint32_t>(s->owned, s->stream, 1, bytes);
+            sc.nodes = dev_alloc<float4>(s->owned, s->stream, 4, bytes, &s->budget);
+            sc.tri_v0 = dev_alloc<float4>(s->owned, s->stream, 1, bytes, &s->budget);
+            sc.tri_e1 = dev_alloc<float4>(s->owned, s->stream, 1, bytes, &s->budget);
+            sc.tri_e2 = dev_alloc<float4>(s->owned, s->stream, 1, bytes, &s->budget);
+            sc.occ_leaf = dev_alloc<uint32_t>(s->owned, s->stream, 1, bytes, &s->budget);
         }
     }
     sc.triangles = T;
@@ -1870,8 +1941,8 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     sc.colored_bounce = o->colored_bounce;
     sc.refine_eps = s->config.refine_epsilon;
     sc.refine_eps2 = sc.refine_eps * sc.refine_eps;
-    s->ctr = dev_alloc<Counters>(s->owned, s->stream, 1, bytes);
-    s->cancel_dev = dev_alloc<uint32_t>(s->owned, s->stream, 1, bytes);
+    s->ctr = dev_alloc<Counters>(s->owned, s->stream, 1, bytes, &s->budget);
+    s->cancel_dev = dev_alloc<uint32_t>(s->owned, s->stream, 1, bytes, &s->budget);
     CK(cudaStreamSynchronize(s->stream));  // allocations and uploads done (the side stream and
                                            // synchronous copies use them from here on)
     for (auto &e : s->marks) CK(cudaEventCreate(&e));
@@ -2009,8 +2080,11 @@ using GatherKernel = void (*)(DevScene, BounceArgs);
 // The gather kernel of a variant, allowed kGatherSmemMax bytes of dynamic shared memory (above
 // the default 48 KB: 16-lane groups of 256 buffered samples need 74 KB with a 64-entry stack).
 constexpr int kGatherSmemMax = 80 * 1024;
-GatherKernel gather_kernel(bool refine, uint32_t minb) {
-    GatherKernel k = refine ? k_gather<true, 6> : minb == 8 ? k_gather<false, 8> : k_gather<false, 6>;
+GatherKernel gather_kernel(bool refine, uint32_t minb, bool count = false) {
+    GatherKernel k = count    ? k_gather<true, false, 6>
+                     : refine ? k_gather<false, true, 6>
+                     : minb == 8 ? k_gather<false, false, 8>
+                                 : k_gather<false, false, 6>;
     CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kGatherSmemMax));
     return k;
 }
@@ -2224,6 +2298,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
     s.report.tuned_stack_depth = s.report.tuned_min_blocks = s.report.tune_trials = 0;
     s.report.ms_tune = 0.0;
     s.report.tuned_gather_lanes = 0;
+    s.report.cancel_stops = 0;
     if (T == 0) {
         // no triangles: every mesh serializes to no words (triangle_words.rs:47-56)
         CK(cudaEventRecord(v0, st));
@@ -2457,7 +2532,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
         CK(cudaEventRecord(v1, st));
     }
     wait(s, progress);
-    if (check_cancel()) return DL_CANCELLED;
+    if (check_cancel()) return cancelled_run(s);
 
     CK(cudaEventRecord(s.marks[4], st));
     // ---- one bounce: photon cubes, gathers, bounce maps (bounce.rs:48-217)
@@ -2512,6 +2587,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
         ba.res = res;
         ba.value = bval;
         ba.ctr = s.ctr;
+        ba.cancel = s.cancel_dev;
         if (bitems) {
             ba.head = P.get<unsigned long long>("gather_head", 1);
             ba.sample_every = 1;
@@ -2524,8 +2600,9 @@ dl_status run(dl_session &s, dl_progress *progress) {
             s.report.tune_trials += g.trials;
             s.report.ms_tune += g.ms;
             CK(cudaMemsetAsync(ba.head, 0, sizeof(unsigned long long), st));
-            gather_kernel(refine, g.minb)<<<g.blocks, kBlock, gather_smem(g.stack_depth, g.lanes, g.buffered), st>>>(
-                sc, ba);
+            // the instrumented variant (counting node visits and triangle tests) when asked
+            gather_kernel(refine, g.minb, s.config.count_visits != 0 && !refine)<<<
+                g.blocks, kBlock, gather_smem(g.stack_depth, g.lanes, g.buffered), st>>>(sc, ba);
             LAUNCHED("k_gather");
             ++s.launches;
         }
@@ -2636,7 +2713,8 @@ dl_status run(dl_session &s, dl_progress *progress) {
     s.mesh_words.resize(M + 1);
     CK(cudaMemcpyAsync(s.mesh_words.data(), mesh_words, (M + 1) * 8ull, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&s.counters, s.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+    wait(s, progress);
+    if (check_cancel()) return cancelled_run(s);
     float ms = 0.0f, vms = 0.0f;
     CK(cudaEventElapsedTime(&ms, e0, e1));
     CK(cudaEventElapsedTime(&vms, v0, v1));
@@ -2653,6 +2731,8 @@ dl_status run(dl_session &s, dl_progress *progress) {
     s.report.bounce_rays = s.counters.bounce_rays;
     s.report.node_visits = s.counters.node_visits;
     s.report.tri_tests = s.counters.tri_tests;
+    s.report.gather_node_visits = s.counters.gather_node_visits;
+    s.report.gather_tri_tests = s.counters.gather_tri_tests;
     s.report.retests = s.counters.retests;
     s.report.kernel_launches = s.launches;
     s.report.device_bytes = s.scene_bytes + P.bytes;
@@ -3262,7 +3342,13 @@ dl_status dl_bake_ex(const dl_bake_input *input, const dl_bake_options *options,
     if (st != DL_OK) return st;
     std::unique_ptr<dl_session> owner(s);
     st = dl_session_run(s, progress);
-    if (st == DL_CANCELLED) g_error = "the bake was cancelled";
+    if (st == DL_CANCELLED) {
+        g_error = "the bake was cancelled";
+        if (report) {
+            *report = s->report;
+            report->ms_total = ms_since(t0);
+        }
+    }
     if (st != DL_OK) return st;
     st = dl_session_result(s, out);
     if (report) {

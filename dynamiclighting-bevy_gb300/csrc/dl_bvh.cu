@@ -687,19 +687,29 @@ __global__ void k_leaf_triangles(DeviceBvhInput in, const uint32_t *idx, DeviceB
 
 uint32_t blocks_for(uint64_t n, uint32_t threads) { return (uint32_t)std::max<uint64_t>(1, (n + threads - 1) / threads); }
 
-// Scratch device memory from the stream-ordered pool, freed on the build's stream when it ends.
+// Scratch device memory from the stream-ordered pool, freed on the build's stream when it ends,
+// counted against the caller's device-memory cap.
 struct Scratch {
     cudaStream_t stream;
+    uint64_t *budget_held;
+    uint64_t cap;
     std::vector<void *> held;
+    uint64_t bytes = 0;
     template <class T>
     T *get(size_t n) {
+        const size_t b = std::max<size_t>(n * sizeof(T), 16);
+        if (budget_held && cap && *budget_held + b > cap)
+            throw DeviceBvhError{cudaErrorMemoryAllocation, "device memory cap (BVH build scratch)"};
         void *p = nullptr;
-        BK(cudaMallocAsync(&p, std::max<size_t>(n * sizeof(T), 16), stream));
+        BK(cudaMallocAsync(&p, b, stream));
         held.push_back(p);
+        bytes += b;
+        if (budget_held) *budget_held += b;
         return static_cast<T *>(p);
     }
     ~Scratch() {
         for (void *p : held) cudaFreeAsync(p, stream);
+        if (budget_held) *budget_held -= std::min(*budget_held, bytes);
     }
 };
 
@@ -710,7 +720,7 @@ void build_bvh_device(const DeviceBvhInput &in, const std::function<void *(size_
     const uint32_t n = in.occluders;
     out = DeviceBvh{};
     if (n == 0) return;
-    Scratch sc{stream, {}};
+    Scratch sc{stream, in.held, in.cap, {}};
     State st;
     st.plo = sc.get<float4>(n);
     st.phi = sc.get<float4>(n);

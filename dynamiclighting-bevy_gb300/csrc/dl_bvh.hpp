@@ -19,6 +19,8 @@ struct DeviceBvhInput {
     const uint32_t *mesh_index_base;   // per mesh: first index in `indices`
     const uint32_t *occ_mesh, *occ_tri;  // per occluder: mesh and triangle
     uint32_t occluders;
+    uint64_t *held = nullptr;  // device bytes the caller holds; the build's scratch counts here
+    uint64_t cap = 0;          // ... and may not take it past this (0: no cap)
 };
 
 struct DeviceBvh {

@@ -594,14 +594,14 @@ struct SunHit {
     f3 value, point;
     bool pending;
 };
-template <bool REFINE>
+template <bool COUNT, bool REFINE>
 __device__ __forceinline__ SunHit sun_hit(const DevScene &sc, const DevLight &l, f3 origin, f3 normal,
                                           const SunGather &g, uint32_t i, int *stack, int stride, Visits *vis) {
     SunHit r{f3{0.0f, 0.0f, 0.0f}, f3{0.0f, 0.0f, 0.0f}, false};
     bool alpha = (l.flags & kLightAlpha) != 0;
     f3 direction = cosine_direction_basis(normal, g.side, g.across, spread(i, g.off, true));
     Hit h;
-    if (!traverse<false, false, REFINE>(sc, origin, direction, INFINITY, alpha, stack, stride, h, vis)) return r;
+    if (!traverse<false, COUNT, REFINE>(sc, origin, direction, INFINITY, alpha, stack, stride, h, vis)) return r;
     f3 face = hit_face_normal(sc, h);
     if (dot(face, direction) >= 0.0f) return r;
     float lit = dot(hit_surface_normal(sc, h, face), l.toward);
@@ -612,21 +612,21 @@ __device__ __forceinline__ SunHit sun_hit(const DevScene &sc, const DevLight &l,
     return r;
 }
 // Whether the shadow ray of a pending sun-bounce sample is open (sun_bounce.rs:67).
-template <bool REFINE>
+template <bool COUNT, bool REFINE>
 __device__ __forceinline__ bool sun_open(const DevScene &sc, const DevLight &l, f3 point, int *stack, int stride,
                                          Visits *vis) {
-    return !occluded<false, REFINE>(sc, point, l.toward, INFINITY, (l.flags & kLightAlpha) != 0, stack, stride, vis);
+    return !occluded<COUNT, REFINE>(sc, point, l.toward, INFINITY, (l.flags & kLightAlpha) != 0, stack, stride, vis);
 }
 // Sample i of gather_sun (sun_bounce.rs:53-71).
-template <bool REFINE>
+template <bool COUNT, bool REFINE>
 __device__ __forceinline__ Contribution sun_sample(const DevScene &sc, const DevLight &l, f3 origin, f3 normal,
                                                   const SunGather &g, uint32_t i, int *stack, int stride,
                                                   Visits *vis) {
     Contribution c{f3{0.0f, 0.0f, 0.0f}, false, 1};
-    SunHit h = sun_hit<REFINE>(sc, l, origin, normal, g, i, stack, stride, vis);
+    SunHit h = sun_hit<COUNT, REFINE>(sc, l, origin, normal, g, i, stack, stride, vis);
     if (!h.pending) return c;
     c.rays = 2;
-    if (sun_open<REFINE>(sc, l, h.point, stack, stride, vis)) {
+    if (sun_open<COUNT, REFINE>(sc, l, h.point, stack, stride, vis)) {
         c.value = h.value;
         c.add = true;
     }

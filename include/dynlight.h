@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define DL_ABI_VERSION 1u
+#define DL_ABI_VERSION 2u
 
 /* Status codes. The first five mirror BakeError (src/bake/input.rs:198-209). */
 typedef enum dl_status {
@@ -176,7 +176,11 @@ typedef struct dl_bake_config {
                                   scene shape (cached per process) */
     uint32_t host_bvh;         /* 1: build the occluder BVH on the host's cores and upload it;
                                   0: build it on the device (the same tree, in milliseconds) */
-    uint32_t reserved[4];
+    uint32_t max_device_mib;   /* cap on the device memory one bake (session) may hold, in MiB:
+                                  scene, BVH and its build scratch, every stage's buffers. An
+                                  allocation past it fails the call with DL_OUT_OF_MEMORY and
+                                  frees what the bake held. 0: no cap */
+    uint32_t reserved[3];
 } dl_bake_config;
 
 /* Timings (device events, milliseconds) and counters of the last bake. */
@@ -213,7 +217,10 @@ typedef struct dl_bake_report {
     uint32_t tune_trials;       /* candidate shapes timed in this run (0: defaults or cached) */
     double ms_tune;             /* host time of those trials */
     uint32_t tuned_gather_lanes; /* lanes sharing one texel's samples in the bounce gather */
-    uint32_t reserved_report;
+    uint32_t cancel_stops;       /* warps of the device work queues that saw the cancel flag and
+                                    stopped claiming work (a cancelled run; 0 otherwise) */
+    uint64_t gather_node_visits; /* BVH nodes visited by the bounce gather (counting config only) */
+    uint64_t gather_tri_tests;   /* triangle tests of the bounce gather (counting config only) */
 } dl_bake_report;
 
 /* LightBvhNode (src/bake/light_bvh.rs:16-22), 32 bytes. */

@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol():
     for name in declared_functions():
         assert hasattr(lib, name), name
     lib.dl_abi_version.restype = C.c_uint32
-    assert lib.dl_abi_version() == 1
+    assert lib.dl_abi_version() == 2
     lib.dl_status_string.restype = C.c_char_p
     assert lib.dl_status_string(1) == b"cancelled"
 
