@@ -274,7 +274,7 @@ def main():
             r = session.report()
             dev_ms.append(r.ms_device)
             vis_ms.append(r.ms_visibility)
-            gather_ms.append(r.ms_stages[4])
+            gather_ms.append(r.ms_gather)
     torch.cuda.synchronize()
     result = session.result()
     rep = session.report()
@@ -307,6 +307,24 @@ def main():
         probe_lib.dl_last_error()
     assert probe_lib.dl_probe_read_bandwidth(local, 1, L2_PROBE_BYTES, 400, C.byref(l1_gbs)) == 0, \
         probe_lib.dl_last_error()
+
+    # the second hot kernel, the bounce gather: node visits x 64 B + triangle tests x 48 B of the
+    # instrumented gather, plus per item the texel, face and value (52 B), over its event time
+    gms = statistics.median(gather_ms)
+    g_bytes = crep.gather_node_visits * 64 + crep.gather_tri_tests * 48 + rep.bounce_items * 52
+    roofline_gather = None
+    if gms > 0 and crep.gather_node_visits:
+        g_achieved = g_bytes / (gms / 1e3) / 1e9
+        roofline_gather = {
+            "bound": "l2", "kernel": "k_gather", "achieved": g_achieved, "peak": l2_gbs.value, "unit": "GB/s",
+            "frac": g_achieved / l2_gbs.value if l2_gbs.value else None,
+            "peak_source": "the same L2 read bandwidth measurement",
+            "limiter": "instruction issue (ncu on the quarter-size outdoor case: issue slots 71 % busy, "
+                       "SIMT efficiency 40 %, L2 throughput 8.4 % of peak)",
+            "algorithmic_bytes_per_launch": int(g_bytes), "ms": gms,
+            "bytes_per_unit": "64 per node visit + 48 per triangle test + 52 per (bounce pair, texel) item",
+            "node_visits": int(crep.gather_node_visits), "tri_tests": int(crep.gather_tri_tests),
+            "items": int(rep.bounce_items)}
 
     # the refined form (binary64 edge re-tests, compensated sums) on the same scene
     refined = dl.Session(inp, opts, form="refined", device=local)
@@ -361,7 +379,7 @@ def main():
                    "l2": "flushed (256 MiB write) before every timed step",
                    "batched_ms": ms, "plain_form_ms": plain_rep.ms_device,
                    "plain_visibility_ms": plain_rep.ms_visibility, "batched_visibility_ms": vis,
-                   "batched_bounce_stage_ms": statistics.median(gather_ms),
+                   "batched_gather_ms": statistics.median(gather_ms),
                    "speedup_batched_vs_plain": plain_rep.ms_device / ms if ms else None,
                    "masks_batched_equal_plain": True,
                    "refined_ms": statistics.median(refined_ms), "refined_retests": refined_retests,
@@ -390,6 +408,7 @@ def main():
                      "bytes_per_unit": "64 per node visit + 48 per triangle test + 76 per (pair, texel) item",
                      "node_visits": int(crep.node_visits), "tri_tests": int(crep.tri_tests),
                      "items": int(crep.work_items)},
+        "roofline_gather": roofline_gather,
     }
     if not args.no_cpu_baseline and world == 1:  # the CPU baseline: rank 0 of a 1-GPU run
         # the oracle on the full workload, all host cores, once; its words are the GPU's

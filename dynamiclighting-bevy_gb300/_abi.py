@@ -74,7 +74,8 @@ class DlBakeReport(C.Structure):
                 ("tuned_stack_depth", C.c_uint32), ("tuned_min_blocks", C.c_uint32),
                 ("tune_trials", C.c_uint32), ("ms_tune", C.c_double),
                 ("tuned_gather_lanes", C.c_uint32), ("cancel_stops", C.c_uint32),
-                ("gather_node_visits", C.c_uint64), ("gather_tri_tests", C.c_uint64)]
+                ("gather_node_visits", C.c_uint64), ("gather_tri_tests", C.c_uint64),
+                ("ms_gather", C.c_double), ("bounce_items", C.c_uint64)]
 
 
 class DlLightBvhNode(C.Structure):

@@ -2279,17 +2279,20 @@ dl_status run(dl_session &s, dl_progress *progress) {
         progress->done = 0;
     }
     auto check_cancel = [&]() { return progress && progress->cancel; };
-    cudaEvent_t e0, e1, v0, v1;
+    cudaEvent_t e0, e1, v0, v1, g0, g1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     CK(cudaEventCreate(&v0));
     CK(cudaEventCreate(&v1));
+    CK(cudaEventCreate(&g0));
+    CK(cudaEventCreate(&g1));
     struct EventGuard {
-        cudaEvent_t *e[4];
+        cudaEvent_t *e[6];
         ~EventGuard() {
             for (auto *x : e) cudaEventDestroy(*x);
         }
-    } guard{{&e0, &e1, &v0, &v1}};
+    } guard{{&e0, &e1, &v0, &v1, &g0, &g1}};
+    bool gathered = false;
     CK(cudaEventRecord(e0, st));
     CK(cudaMemsetAsync(s.ctr, 0, sizeof(Counters), st));
     CK(cudaMemsetAsync(s.cancel_dev, 0, 4, st));
@@ -2299,6 +2302,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
     s.report.ms_tune = 0.0;
     s.report.tuned_gather_lanes = 0;
     s.report.cancel_stops = 0;
+    s.report.bounce_items = 0;
     if (T == 0) {
         // no triangles: every mesh serializes to no words (triangle_words.rs:47-56)
         CK(cudaEventRecord(v0, st));
@@ -2312,7 +2316,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
         s.out_words = 0;
         s.words_dev = nullptr;
         s.texels = 0;
-        s.report.ms_device = s.report.ms_visibility = 0.0;
+        s.report.ms_device = s.report.ms_visibility = s.report.ms_gather = 0.0;
         s.report.pairs = 0;
         s.report.kernel_launches = s.launches;
         s.have_result = true;
@@ -2570,6 +2574,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
         LAUNCHED("k_item_counts");
         scan_u32(s, bcnt, bitem_off, bcount + 1);
         const uint32_t bitems = read_back(s, bitem_off + bcount);
+        s.report.bounce_items = bitems;
         s.launches += 3;
         float4 *bval = P.get<float4>("bval", bitems);
         BounceArgs ba{};
@@ -2601,9 +2606,12 @@ dl_status run(dl_session &s, dl_progress *progress) {
             s.report.ms_tune += g.ms;
             CK(cudaMemsetAsync(ba.head, 0, sizeof(unsigned long long), st));
             // the instrumented variant (counting node visits and triangle tests) when asked
+            CK(cudaEventRecord(g0, st));
             gather_kernel(refine, g.minb, s.config.count_visits != 0 && !refine)<<<
                 g.blocks, kBlock, gather_smem(g.stack_depth, g.lanes, g.buffered), st>>>(sc, ba);
             LAUNCHED("k_gather");
+            CK(cudaEventRecord(g1, st));
+            gathered = true;
             ++s.launches;
         }
         // windows per (mesh, bounce light)
@@ -2720,6 +2728,9 @@ dl_status run(dl_session &s, dl_progress *progress) {
     CK(cudaEventElapsedTime(&vms, v0, v1));
     s.report.ms_device = ms;
     s.report.ms_visibility = vms;
+    float gms = 0.0f;
+    if (gathered) CK(cudaEventElapsedTime(&gms, g0, g1));
+    s.report.ms_gather = gms;
     for (int k = 0; k < 8; ++k) {
         float ms_k = 0.0f;
         CK(cudaEventElapsedTime(&ms_k, s.marks[k], s.marks[k + 1]));

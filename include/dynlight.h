@@ -221,6 +221,8 @@ typedef struct dl_bake_report {
                                     stopped claiming work (a cancelled run; 0 otherwise) */
     uint64_t gather_node_visits; /* BVH nodes visited by the bounce gather (counting config only) */
     uint64_t gather_tri_tests;   /* triangle tests of the bounce gather (counting config only) */
+    double ms_gather;            /* device time of the bounce gather kernel alone (0: no gather) */
+    uint64_t bounce_items;       /* (bounce pair, texel) items of the gather queue */
 } dl_bake_report;
 
 /* LightBvhNode (src/bake/light_bvh.rs:16-22), 32 bytes. */
