@@ -171,7 +171,7 @@ def precision_slice(name, device):
     t0 = time.perf_counter()
     ref64 = oracle.bake_ex(inp, opts, mode=oracle.F64, threads=os.cpu_count() or 1, bounce_maps=True)
     out = {"slice": desc, "fp64_oracle_s": round(time.perf_counter() - t0, 2)}
-    for form in ("batched", "refined"):
+    for form in ("batched", "refined", "bounce_refined"):
         s = dl.Session(inp, opts, form=form, device=device)
         try:
             s.run()
@@ -335,6 +335,17 @@ def main():
             refined_ms.append(refined.report().ms_device)
     refined_retests = int(refined.report().retests)
     refined.close()
+    # the bounce-refined form: the batched form's masks with the refined form's bounce
+    hybrid = dl.Session(inp, opts, form="bounce_refined", device=local)
+    hybrid_ms = []
+    for i in range(3):
+        hybrid.run()
+        if i:
+            hybrid_ms.append(hybrid.report().ms_device)
+    from dynlight_gb300 import compare
+    hybrid_flips = compare.bit_flips(hybrid.result(), result)
+    hybrid_masks_equal = all(v["flips"] == 0 for k, v in hybrid_flips.items() if k != "bounce")
+    hybrid.close()
     traffic = None
     traffic_path = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(traffic_path):  # DRAM bytes per launch from an ncu capture (profiles/)
@@ -383,6 +394,8 @@ def main():
                    "speedup_batched_vs_plain": plain_rep.ms_device / ms if ms else None,
                    "masks_batched_equal_plain": True,
                    "refined_ms": statistics.median(refined_ms), "refined_retests": refined_retests,
+                   "bounce_refined_ms": statistics.median(hybrid_ms),
+                   "bounce_refined_masks_equal_batched": hybrid_masks_equal,
                    "launch_shape": {"chunk_texels": rep.tuned_chunk_texels, "sample_lanes": rep.tuned_sample_lanes,
                                     "blocks_per_sm": rep.tuned_blocks_per_sm,
                                     "stack_depth": rep.tuned_stack_depth, "launch_bound_blocks": rep.tuned_min_blocks,
@@ -423,6 +436,7 @@ def main():
             p = line["config"]["precision"]
             line["config"]["bounce_err_vs_fp64_bitexact"] = p["batched"]["bounce_max_rel_err_vs_fp64"]
             line["config"]["bounce_err_vs_fp64_refined"] = p["refined"]["bounce_max_rel_err_vs_fp64"]
+            line["config"]["bounce_err_vs_fp64_bounce_refined"] = p["bounce_refined"]["bounce_max_rel_err_vs_fp64"]
     print(json.dumps(line))
 
 

@@ -31,9 +31,10 @@ POINT, RECTANGLE, TUBE, SUN, SKY = 0, 1, 2, 3, 4
 DIRECT, SINGLE_BOUNCE = 0, 1
 TRANSPARENCY_DISABLED, TRANSPARENCY_ENABLED, TRANSPARENCY_ENABLED_MAX = 0, 1, 2
 LIGHTING_ONLY, DISTANCE_CUBES, ANGULAR = 0, 1, 2
-FORM_BATCHED, FORM_PLAIN, FORM_REFINED = 0, 1, 2
+FORM_BATCHED, FORM_PLAIN, FORM_REFINED, FORM_BOUNCE_REFINED = 0, 1, 2, 3
 DEFAULT_REFINE_EPSILON = 1e-4  # dl_bake_config.refine_epsilon when left 0
-FORMS = {"batched": FORM_BATCHED, "plain": FORM_PLAIN, "refined": FORM_REFINED}
+FORMS = {"batched": FORM_BATCHED, "plain": FORM_PLAIN, "refined": FORM_REFINED,
+         "bounce_refined": FORM_BOUNCE_REFINED}
 
 ERROR_KINDS = {1: "Cancelled", 2: "DuplicateId", 3: "InvalidMesh", 4: "InvalidLight",
                5: "InvalidOptions"}

@@ -1730,7 +1730,7 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     auto s = std::make_unique<dl_session>();
     s->options = *o;
     if (cfg) s->config = *cfg;
-    if (s->config.form > DL_FORM_REFINED) {
+    if (s->config.form > DL_FORM_BOUNCE_REFINED) {
         g_error = "unknown bake form " + std::to_string(s->config.form);
         return DL_INVALID_ARGUMENT;
     }
@@ -2267,6 +2267,9 @@ dl_status run(dl_session &s, dl_progress *progress) {
     Pool &P = s.pool;
     cudaStream_t st = s.stream;
     const bool refine = s.config.form == DL_FORM_REFINED;
+    // the refined predicates and compensated sums for the bounce stages only (photon cubes and
+    // gathers): masks stay the bit-exact forms', bounce follows the refined form
+    const bool refine_bounce = refine || s.config.form == DL_FORM_BOUNCE_REFINED;
     s.launches = 0;
     s.have_result = false;
     s.bounce_woff = nullptr;
@@ -2553,7 +2556,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
         if (cubes) {
             uint32_t *cube_lights = P.get<uint32_t>("cube_lights", cubes);
             CK(cudaMemcpyAsync(cube_lights, hs.cube_lights.data(), cubes * 4ull, cudaMemcpyHostToDevice, st));
-            auto photon = refine ? k_photons<true> : k_photons<false>;
+            auto photon = refine_bounce ? k_photons<true> : k_photons<false>;
             photon<<<grid_for(photons_n), kBlock, 0, st>>>(sc, cube_lights, cubes, res, photons, s.ctr);
             LAUNCHED("k_photons");
             ++s.launches;
@@ -2596,7 +2599,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
         if (bitems) {
             ba.head = P.get<unsigned long long>("gather_head", 1);
             ba.sample_every = 1;
-            GatherTune g = gather_tune(s, ba, bcount, refine, progress);
+            GatherTune g = gather_tune(s, ba, bcount, refine_bounce, progress);
             ba.lanes = g.lanes;
             ba.stack_depth = g.stack_depth;
             ba.buffered = g.buffered;
@@ -2607,7 +2610,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
             CK(cudaMemsetAsync(ba.head, 0, sizeof(unsigned long long), st));
             // the instrumented variant (counting node visits and triangle tests) when asked
             CK(cudaEventRecord(g0, st));
-            gather_kernel(refine, g.minb, s.config.count_visits != 0 && !refine)<<<
+            gather_kernel(refine_bounce, g.minb, s.config.count_visits != 0 && !refine_bounce)<<<
                 g.blocks, kBlock, gather_smem(g.stack_depth, g.lanes, g.buffered), st>>>(sc, ba);
             LAUNCHED("k_gather");
             CK(cudaEventRecord(g1, st));

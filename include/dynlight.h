@@ -155,7 +155,11 @@ enum {
                             device work queue, launched from a CUDA graph */
     DL_FORM_PLAIN = 1,   /* one launch per mesh, a warp per triangle looping over its lights and
                             texels: the reference's loop order on the GPU */
-    DL_FORM_REFINED = 2  /* the batched form with binary64 edge re-tests and compensated sums */
+    DL_FORM_REFINED = 2, /* the batched form with binary64 edge re-tests and compensated sums */
+    DL_FORM_BOUNCE_REFINED = 3 /* the batched form's bit-exact visibility and burial (its masks
+                            are the BATCHED form's, bit for bit) with the REFINED form's photon
+                            cubes, bounce gathers and compensated bounce sums (its bounce follows
+                            an FP64 bake) */
 };
 
 /* Launch configuration of one bake; zero-initialise for the defaults. */

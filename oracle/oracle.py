@@ -65,7 +65,7 @@ def lib():
 
 # Precision modes of bake_ex: the reference's binary32, the GPU library's refined form, and the
 # FP64 oracle (binary64 ray/triangle tests, sums and fractions over the same binary32 samples).
-F32, REFINED, F64 = 0, 1, 2
+F32, REFINED, F64, REFINED_BOUNCE = 0, 1, 2, 3
 
 
 DIR_FN = C.CFUNCTYPE(C.c_int, C.POINTER(C.c_float), C.c_float)

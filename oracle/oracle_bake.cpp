@@ -369,6 +369,7 @@ static V3 reflected(const Scene &sc, V3 albedo) { return sc.options->colored_bou
 
 static uint64_t gather_triangle(const Scene &sc, const std::vector<SurfaceTexel> &texels, const Setup &s,
                                 const Prepared &p, uint32_t slot, std::vector<GatheredTexel> &out) {
+    BounceScope bounce_stage;
     if (is_zero(s.face_normal)) return 0;
     const Light &light = sc.lights[slot];
     const PhotonCube &cube = sc.cubes[slot];
@@ -409,6 +410,7 @@ static uint64_t gather_triangle(const Scene &sc, const std::vector<SurfaceTexel>
 
 static uint64_t gather_sun(const Scene &sc, const std::vector<SurfaceTexel> &texels, const Setup &s,
                            const Prepared &p, uint32_t slot, std::vector<GatheredTexel> &out) {
+    BounceScope bounce_stage;
     if (is_zero(s.face_normal)) return 0;
     const Light &light = sc.lights[slot];
     V3 toward = sc.sun_toward[slot];
@@ -966,17 +968,19 @@ const char *oracle_last_error(void) { return g_error.c_str(); }
 
 // Bakes with `threads` worker threads (0: all cores). `brute_force` tests every occluder per ray.
 // `mode` is a Precision (0 the reference's binary32, 1 the refined form with re-test margin
-// `eps`, 2 the FP64 oracle); `retests` gets the refined form's binary64 re-tests.
+// `eps`, 2 the FP64 oracle, 3 the bounce-refined form: binary32 but in the bounce stages, which
+// run refined); `retests` gets the refined form's binary64 re-tests.
 int oracle_bake_ex(const dl_bake_input *in, const dl_bake_options *o, const dl_progress *progress, uint32_t threads,
                    uint32_t brute_force, uint32_t mode, float eps, dl_baked_scene **out, uint64_t *burial_rays,
                    uint64_t *photon_rays, uint64_t *retests) {
-    if (mode > PREC_F64 || !(eps >= 0.0f)) {
+    if (mode > PREC_REFINED_BOUNCE || !(eps >= 0.0f)) {
         g_error = "invalid precision mode";
         *out = nullptr;
         return DL_INVALID_OPTIONS;
     }
     thread_count() = threads ? threads : std::max(1u, std::thread::hardware_concurrency());
-    precision().mode = (Precision)mode;
+    precision().mode = mode == PREC_REFINED_BOUNCE ? PREC_F32 : (Precision)mode;
+    precision().bounce = mode == PREC_REFINED_BOUNCE ? PREC_REFINED : (Precision)mode;
     precision().eps = eps;
     precision().eps2 = eps * eps;
     retest_count().store(0);

@@ -91,6 +91,7 @@ struct PhotonCube {
 };
 // photon (bounce.rs:88-115)
 inline Photon make_photon(const Light &light, const Occluders &occ, V3 dir) {
+    BounceScope bounce_stage;
     SurfaceHit hit;
     if (!occ.closest_hit(light.position(), dir, light.l->radius, light.alpha_tested(), hit))
         return Photon{light.l->radius, {0, 0, 0}, {0, 0, 0}};

@@ -189,7 +189,7 @@ inline bool adaptive_share(const P *probes, int probe_count, Sampling s, SpreadP
         return true;
     }
     if (total.value() > 0.0) {
-        fraction = precision().mode == PREC_F64 ? lit_sum.d / total.d : (double)(lit_sum.s / total.s);
+        fraction = active_mode() == PREC_F64 ? lit_sum.d / total.d : (double)(lit_sum.s / total.s);
         return true;
     }
     return false;
@@ -279,7 +279,7 @@ inline Visibility sky_visibility(V3 normal, uint32_t samples, Rng &rng, Occ occl
     uint32_t open = 0;
     for (uint32_t taken = 0; taken < samples; ++taken)
         if (!occluded(cosine_direction(normal, spread(taken, offset, true)))) ++open;
-    double fraction = precision().mode == PREC_F64 ? (double)open / (double)std::max(samples, 1u)
+    double fraction = active_mode() == PREC_F64 ? (double)open / (double)std::max(samples, 1u)
                                                    : (double)((float)open / (float)std::max(samples, 1u));
     return {true, fraction, samples};
 }

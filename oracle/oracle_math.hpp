@@ -252,16 +252,30 @@ inline V3 on_unit_sphere(Rng &rng) {
 // in binary64 and soft-visibility weights and bounce gathers use Kahan sums. F64 is the FP64
 // oracle: every ray/triangle test, the soft-visibility and bounce sums and the fractions they
 // give in binary64, over the same binary32 samples (origins, directions, weights, integrands),
-// so it measures the predicates and the accumulation, not the sampling.
-enum Precision : uint32_t { PREC_F32 = 0, PREC_REFINED = 1, PREC_F64 = 2 };
+// so it measures the predicates and the accumulation, not the sampling. REFINED_BOUNCE restates
+// the library's bounce-refined form: F32 everywhere but in the bounce stages (photon cubes and
+// gathers), which run as REFINED.
+enum Precision : uint32_t { PREC_F32 = 0, PREC_REFINED = 1, PREC_F64 = 2, PREC_REFINED_BOUNCE = 3 };
 struct PrecisionMode {
-    Precision mode = PREC_F32;
+    Precision mode = PREC_F32;    // outside the bounce stages
+    Precision bounce = PREC_F32;  // inside them
     float eps = 1.0e-5f, eps2 = 1.0e-10f;
 };
 inline PrecisionMode &precision() {
     static PrecisionMode p;
     return p;
 }
+// Whether this thread is inside a bounce stage (BounceScope), and the mode in force there.
+inline bool &in_bounce_stage() {
+    static thread_local bool on = false;
+    return on;
+}
+inline Precision active_mode() { return in_bounce_stage() ? precision().bounce : precision().mode; }
+struct BounceScope {
+    bool was;
+    BounceScope() : was(in_bounce_stage()) { in_bounce_stage() = true; }
+    ~BounceScope() { in_bounce_stage() = was; }
+};
 
 struct D3 {
     double x, y, z;
@@ -277,7 +291,7 @@ struct Acc {
     float s = 0.0f, c = 0.0f;
     double d = 0.0;
     void add(float x) {
-        switch (precision().mode) {
+        switch (active_mode()) {
         case PREC_F64: d += (double)x; break;
         case PREC_REFINED: {
             float y = x - c;
@@ -289,7 +303,7 @@ struct Acc {
         default: s = s + x;
         }
     }
-    double value() const { return precision().mode == PREC_F64 ? d : (double)s; }
+    double value() const { return active_mode() == PREC_F64 ? d : (double)s; }
 };
 struct Acc3 {
     Acc x, y, z;
@@ -301,7 +315,7 @@ struct Acc3 {
     // sum * scale / n: binary32 in F32/REFINED (the reference's `sum * intensity / samples`),
     // binary64 rounded once in F64
     V3 mean(float scale, uint32_t n) const {
-        if (precision().mode == PREC_F64)
+        if (active_mode() == PREC_F64)
             return V3{(float)(x.d * scale / n), (float)(y.d * scale / n), (float)(z.d * scale / n)};
         return V3{x.s, y.s, z.s} * scale / (float)n;
     }

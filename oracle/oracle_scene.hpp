@@ -94,7 +94,7 @@ inline uint8_t level(float fraction, uint32_t bits) {
 // level() of a fraction held in binary64: rounded in binary64 in the F64 mode, else level() of
 // the binary32 fraction
 inline uint8_t level_of(double fraction, uint32_t bits) {
-    if (precision().mode != PREC_F64) return level((float)fraction, bits);
+    if (active_mode() != PREC_F64) return level((float)fraction, bits);
     double max = (double)((1u << bits) - 1);
     double v = std::round(std::min(std::max(fraction, 0.0), 1.0) * max);
     return (uint8_t)v;
@@ -500,7 +500,7 @@ inline bool intersect_refined(const V3 v[3], V3 o, V3 d, float max, float &t_out
 }
 
 inline bool intersect(const V3 v[3], V3 o, V3 d, float max, float &t_out, V3 &w_out) {
-    switch (precision().mode) {
+    switch (active_mode()) {
     case PREC_F64: return intersect_f64(v, o, d, max, t_out, w_out);
     case PREC_REFINED: return intersect_refined(v, o, d, max, t_out, w_out);
     default: return intersect_f32(v, o, d, max, t_out, w_out);
@@ -688,7 +688,7 @@ struct Occluders {
         auto consider = [&](uint32_t i) {
             float t;
             V3 w;
-            if (precision().mode == PREC_REFINED) {
+            if (active_mode() == PREC_REFINED) {
                 // candidates ordered by their binary64 distance, barycentrics from it too
                 if (!intersect(triangles[i].v, o, d, max, t, w)) return;
                 retest_count().fetch_add(1, std::memory_order_relaxed);
@@ -726,7 +726,7 @@ struct Occluders {
             }
         }
         if (!found) return false;
-        if (precision().mode != PREC_F32) {
+        if (active_mode() != PREC_F32) {
             // the winning test's own barycentrics (a re-test with max = infinity could take the
             // other precision path)
             out = SurfaceHit{best, best_i, best_w};

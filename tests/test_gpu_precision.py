@@ -64,6 +64,32 @@ def test_refined_form_matches_the_refined_oracle(stress):
     assert report.retests > 0
 
 
+def test_bounce_refined_form_matches_its_oracle_and_keeps_the_exact_masks(stress):
+    """The bounce-refined form against the oracle's bounce-refined mode, word for word and bounce
+    map for bounce map; its masks equal the batched form's bit for bit and its bounce is within
+    1e-4 of the FP64 oracle, the two clauses of the target in one bake."""
+    inp, opts, bakes = stress
+    want = oracle.bake_ex(inp, opts, mode=oracle.REFINED_BOUNCE, eps=dl.DEFAULT_REFINE_EPSILON, bounce_maps=True)
+    scene, maps, report = _gpu(inp, opts, "bounce_refined")
+    assert_same(scene, want["scene"])
+    _maps_equal(maps, want["maps"])
+    assert report.retests > 0
+    exact, _, _ = _gpu(inp, opts, "batched")
+    flips = compare.bit_flips(scene, exact)
+    assert all(v["flips"] == 0 for k, v in flips.items() if k != "bounce"), flips
+    err = compare.bounce_error(maps, bakes["f64"]["maps"])
+    assert err["maps"] > 0 and err["max"] <= 1e-4, err
+    # every light kind, with a local and a sun bounce
+    inp, opts = fx.determinism_room()
+    for light, n in ((inp.lights[0], 16), (inp.lights[7], 32)):
+        light.illumination = dl.SINGLE_BOUNCE
+        light.bounce = dl.BakeBounce(samples=n)
+    opts.photon_cube_resolution = 64
+    want = oracle.bake_ex(inp, opts, mode=oracle.REFINED_BOUNCE, eps=dl.DEFAULT_REFINE_EPSILON)["scene"]
+    got, _, _ = _gpu(inp, opts, "bounce_refined")
+    assert_same(got, want)
+
+
 @pytest.mark.parametrize("eps", [1e-7, 1e-6, 1e-5])
 def test_refined_epsilon_sweep_matches_the_oracle(eps):
     inp, opts = scenes.precision_stress(grid=40, chunks=2, boxes=8, decals=600, slivers=120, lights=10,

@@ -94,7 +94,7 @@ def stress_bakes():
     inp, opts = _stress()
     return inp, opts, {name: oracle.bake_ex(inp, opts, mode=mode, eps=1e-5, bounce_maps=True)
                        for name, mode in (("f32", oracle.F32), ("refined", oracle.REFINED),
-                                          ("f64", oracle.F64))}
+                                          ("f64", oracle.F64), ("bounce", oracle.REFINED_BOUNCE))}
 
 
 def _total(flips):
@@ -118,6 +118,20 @@ def test_refined_mode_is_closer_to_fp64(stress_bakes):
     assert err["maps"] > 0 and err["max"] <= 1e-4
     # every mode samples the same rays, so the statistics agree
     assert bakes["refined"]["scene"].stats == bakes["f32"]["scene"].stats == bakes["f64"]["scene"].stats
+
+
+def test_bounce_refined_mode_keeps_the_binary32_masks(stress_bakes):
+    """The bounce-refined form: its masks are the reference restatement's bit for bit (binary32
+    visibility and burial), its bounce is the refined form's (refined photons and gathers, Kahan
+    sums), so one bake meets both clauses: bit-identical masks and bounce near FP64."""
+    _, _, bakes = stress_bakes
+    hybrid, f32 = bakes["bounce"]["scene"], bakes["f32"]["scene"]
+    flips = compare.bit_flips(hybrid, f32)
+    assert {k: v["flips"] for k, v in flips.items() if k != "bounce"} == {k: 0 for k in flips if k != "bounce"}
+    assert bakes["bounce"]["retests"] > 0
+    err = compare.bounce_error(bakes["bounce"]["maps"], bakes["f64"]["maps"])
+    assert err["maps"] > 0 and err["max"] <= 1e-4
+    assert hybrid.stats == f32.stats
 
 
 def test_bit_flips_count_planted_differences(stress_bakes):
