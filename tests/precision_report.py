@@ -82,7 +82,8 @@ def outdoor_report():
            "oracle_f32_s": round(t32, 1), "oracle_f64_s": round(t64, 1),
            "oracle_f32_vs_f64_flips": compare.bit_flips(ref32["scene"], ref64["scene"]),
            "oracle_f32_bounce_error_vs_f64": compare.bounce_error(ref32["maps"], ref64["maps"])}
-    for form, tuning in (("batched", {}), ("plain", {}), ("refined", {}), ("refined eps 1e-5", {"refine_epsilon": 1e-5})):
+    for form, tuning in (("batched", {}), ("plain", {}), ("refined", {}), ("refined eps 1e-5", {"refine_epsilon": 1e-5}),
+                         ("bounce_refined", {})):
         scene, maps, rep = gpu_with_maps(inp, opts, form.split()[0], **tuning)
         out[form] = {"words_equal_reference": bool(scene.words_equal(ref32["scene"])),
                      "stats_equal_reference": scene.stats == ref32["scene"].stats,
