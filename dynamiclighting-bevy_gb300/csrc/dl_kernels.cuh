@@ -500,9 +500,10 @@ __device__ __forceinline__ f3 slerp3(f3 a, f3 b, float s) {
     const float eps = 1.1920928955078125e-7f;  // f32::EPSILON
     if (fabsf(d) < 1.0f - 3.0f * eps) {
         const float angle = acos_approx(d);
-        const float angle_sin = sin_f(angle);
-        const float t1 = sin_f(angle * (1.0f - s)) / angle_sin;
-        const float t2 = sin_f(angle * s) / angle_sin * (la / lb);
+        // three sines in a row: one shared out-of-line copy keeps the gather's code small
+        const float angle_sin = sin_f_outline(angle);
+        const float t1 = sin_f_outline(angle * (1.0f - s)) / angle_sin;
+        const float t2 = sin_f_outline(angle * s) / angle_sin * (la / lb);
         return scale(add(scale(a, t1), scale(b, t2)), 1.0f + s * (lb / la - 1.0f));
     }
     if (d < 0.0f) {

@@ -20,8 +20,10 @@
 
 #if defined(__CUDACC__)
 #define DL_HD __host__ __device__ __forceinline__
+#define DL_HD_OUTLINE static __host__ __device__ __noinline__  // one shared copy per unit
 #else
 #define DL_HD inline
+#define DL_HD_OUTLINE inline
 #endif
 
 namespace dl {
@@ -292,6 +294,15 @@ constexpr float kPio2F1 = 1.570796012878418f;      // 0x1.921fb0p+0
 constexpr float kPio2F2 = 3.139164164167596e-07f;  // 0x1.5110b0p-22
 constexpr float kPio2F3 = 6.223371969669989e-14f;  // 0x1.184698p-44
 
+// The binary64 path of sincos_f and sin_f, out of line: it runs for a small share of arguments,
+// so one shared copy keeps the call sites' code (and the instruction cache they need) small.
+DL_HD_OUTLINE void sincos_rounded_b64(float x, float &s, float &c) {
+    double sd, cd;
+    sincos_d((double)x, sd, cd);
+    s = (float)sd;
+    c = (float)cd;
+}
+
 DL_HD void sincos_f(float x, float &s, float &c) {
     if (!isfinite(x)) {
         s = c = NAN;
@@ -318,10 +329,7 @@ DL_HD void sincos_f(float x, float &s, float &c) {
         }
     }
     // binary64 path: Cody–Waite reduction and Taylor series in binary64, one rounding
-    double sd, cd;
-    sincos_d((double)x, sd, cd);
-    s = (float)sd;
-    c = (float)cd;
+    sincos_rounded_b64(x, s, c);
 }
 // sin alone: the reduction of sincos_f and only the polynomial the quadrant needs (sin of the
 // reduced argument for even quadrants, cos for odd ones), its own rounding test, the same
@@ -341,10 +349,13 @@ DL_HD float sin_f(float x) {
         }
     }
     if (!isfinite(x)) return NAN;
-    double sd, cd;
-    sincos_d((double)x, sd, cd);
-    return (float)sd;
+    float s, c;
+    sincos_rounded_b64(x, s, c);
+    return s;
 }
+// sin_f as one shared out-of-line copy, for call sites that take several sines in a row (the
+// bounce slerp's three).
+DL_HD_OUTLINE float sin_f_outline(float x) { return sin_f(x); }
 DL_HD float tan_f(float x) {
     if (!isfinite(x)) return NAN;
     double s, c;
