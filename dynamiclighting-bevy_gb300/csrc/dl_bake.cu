@@ -1722,6 +1722,69 @@ dl_status cancelled_run(dl_session &s) {
     return DL_CANCELLED;
 }
 
+// Host buffers of freed results' words, handed to the next result. They are pinned (page-locked)
+// when the driver allows it, so that the download runs as a DMA copy at the link's rate instead
+// of through the driver's staging buffers, and a reused buffer needs no first-touch page faults
+// either. At most kCacheBytes are held.
+struct WordCache {
+    static constexpr size_t kCacheBytes = size_t(2) << 30;
+    struct Buffer {
+        size_t cap;  // words
+        uint32_t *p;
+        bool pinned;
+    };
+    std::mutex lock;
+    std::vector<Buffer> free;
+    size_t held = 0;
+    static void release(const Buffer &b) {
+        if (b.pinned) cudaFreeHost(b.p);  // fails harmlessly once the runtime has shut down at exit
+        else delete[] b.p;
+    }
+    Buffer take(size_t n) {
+        {
+            std::lock_guard<std::mutex> guard(lock);
+            size_t best = free.size();
+            for (size_t i = 0; i < free.size(); ++i)
+                if (free[i].cap >= n && (best == free.size() || free[i].cap < free[best].cap)) best = i;
+            if (best < free.size()) {
+                Buffer b = free[best];
+                free.erase(free.begin() + best);
+                held -= b.cap * 4;
+                return b;
+            }
+        }
+        size_t cap = n ? n : 1;
+        void *p = nullptr;
+        if (cudaHostAlloc(&p, cap * 4, cudaHostAllocPortable) == cudaSuccess) return Buffer{cap, (uint32_t *)p, true};
+        cudaGetLastError();  // no pinned memory to be had: a pageable buffer (a slower copy)
+        return Buffer{cap, new uint32_t[cap], false};
+    }
+    void clear() {
+        std::lock_guard<std::mutex> guard(lock);
+        for (const Buffer &b : free) release(b);
+        free.clear();
+        held = 0;
+    }
+    void give(const Buffer &b) {
+        std::lock_guard<std::mutex> guard(lock);
+        while (held + b.cap * 4 > kCacheBytes && !free.empty()) {  // drop the oldest
+            held -= free.front().cap * 4;
+            release(free.front());
+            free.erase(free.begin());
+        }
+        if (b.cap * 4 > kCacheBytes) {
+            release(b);
+            return;
+        }
+        free.push_back(b);
+        held += b.cap * 4;
+    }
+};
+WordCache &word_cache() {
+    static WordCache *c = new WordCache;  // never destroyed: results may be freed during exit
+    return *c;
+}
+
 // `progress`, when given, is checked for cancellation once validation has passed and before the
 // first CUDA call: as in the reference (baker.rs:32-55), invalid input reports its own error even
 // when the bake was already cancelled.
@@ -1812,21 +1875,57 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
         }
     }
     uint32_t V = vbase[M], I = ibase[M], T = tbase[M];
-    std::vector<float> pos(V * 3), nrm(V * 3, 0.0f), uv1(V * 2), uv0(V * 2, 0.0f);
-    std::vector<uint32_t> idx(I), tri_mesh(T);
-    for (uint32_t m = 0; m < M; ++m) {
+    // The per-vertex and per-index arrays are flattened by the host's cores into one pinned
+    // staging buffer (reused across sessions through the result-word cache), so that their
+    // uploads run as DMA copies; the buffer goes back once the stream has drained.
+    struct Staging {
+        WordCache::Buffer b;
+        cudaStream_t stream;
+        ~Staging() {
+            if (stream) cudaStreamSynchronize(stream);
+            word_cache().give(b);
+        }
+    } staging{word_cache().take((size_t)V * 10 + I + T + 1), s->stream};
+    float *pos = reinterpret_cast<float *>(staging.b.p), *nrm = pos + (size_t)V * 3, *uv1 = nrm + (size_t)V * 3,
+          *uv0 = uv1 + (size_t)V * 2;
+    uint32_t *idx = reinterpret_cast<uint32_t *>(uv0 + (size_t)V * 2), *tri_mesh = idx + I;
+    auto flatten = [&](uint32_t m) {
         const dl_mesh &mm = *h.meshes[m];
-        std::memcpy(&pos[vbase[m] * 3], mm.positions, mm.vertex_count * 12ull);
-        if (mm.normals) std::memcpy(&nrm[vbase[m] * 3], mm.normals, mm.vertex_count * 12ull);
+        std::memcpy(&pos[(size_t)vbase[m] * 3], mm.positions, mm.vertex_count * 12ull);
+        if (mm.normals) std::memcpy(&nrm[(size_t)vbase[m] * 3], mm.normals, mm.vertex_count * 12ull);
+        else std::memset(&nrm[(size_t)vbase[m] * 3], 0, mm.vertex_count * 12ull);
         for (uint32_t v = 0; v < mm.vertex_count; ++v) {
             float a = mm.uv1[v * 2], b = mm.uv1[v * 2 + 1];
             bool ok = std::isfinite(a) && std::isfinite(b);  // mesh_builder.rs:30-40
-            uv1[(vbase[m] + v) * 2] = ok ? a : 0.0f;
-            uv1[(vbase[m] + v) * 2 + 1] = ok ? b : 0.0f;
+            uv1[((size_t)vbase[m] + v) * 2] = ok ? a : 0.0f;
+            uv1[((size_t)vbase[m] + v) * 2 + 1] = ok ? b : 0.0f;
         }
-        if (mm.uv0) std::memcpy(&uv0[vbase[m] * 2], mm.uv0, mm.vertex_count * 8ull);
+        if (mm.uv0) std::memcpy(&uv0[(size_t)vbase[m] * 2], mm.uv0, mm.vertex_count * 8ull);
+        else std::memset(&uv0[(size_t)vbase[m] * 2], 0, mm.vertex_count * 8ull);
         std::memcpy(&idx[ibase[m]], mm.indices, mm.index_count * 4ull);
         for (uint32_t t = tbase[m]; t < tbase[m + 1]; ++t) tri_mesh[t] = m;
+    };
+    {
+        // meshes split into contiguous runs of about equal vertex and index counts, one per thread
+        const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        const uint64_t per = ((uint64_t)V + I) / hw + 1;
+        std::vector<uint32_t> cut{0};
+        uint64_t acc = 0;
+        for (uint32_t m = 0; m < M; ++m) {
+            acc += (uint64_t)h.meshes[m]->vertex_count + h.meshes[m]->index_count;
+            if (acc >= per && m + 1 < M) {
+                cut.push_back(m + 1);
+                acc = 0;
+            }
+        }
+        cut.push_back(M);
+        std::vector<std::thread> pool;
+        for (size_t r = 0; r + 2 < cut.size(); ++r)
+            pool.emplace_back([&, r] {
+                for (uint32_t m = cut[r]; m < cut[r + 1]; ++m) flatten(m);
+            });
+        for (uint32_t m = cut[cut.size() - 2]; m < cut.back(); ++m) flatten(m);
+        for (auto &t : pool) t.join();
     }
     s->grid_off.resize(M + 1);
     s->grid_words = 0;
@@ -1860,11 +1959,11 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
     up(albedo.data(), M * 12ull, sc.mesh_albedo);
     up(alpha.data(), M * 16ull, sc.mesh_alpha);
     up(alpha_pool.data(), alpha_pool.size(), sc.alpha_pool);
-    up(pos.data(), pos.size() * 4, sc.positions);
-    up(nrm.data(), nrm.size() * 4, sc.normals);
-    up(uv1.data(), uv1.size() * 4, sc.uv1);
-    up(uv0.data(), uv0.size() * 4, sc.uv0);
-    up(idx.data(), idx.size() * 4, sc.indices);
+    up(pos, (size_t)V * 12, sc.positions);
+    up(nrm, (size_t)V * 12, sc.normals);
+    up(uv1, (size_t)V * 8, sc.uv1);
+    up(uv0, (size_t)V * 8, sc.uv0);
+    up(idx, (size_t)I * 4, sc.indices);
     double ms_bvh_device = 0.0;
     if (host_bvh) {
         std::vector<uint32_t> occ_leaf(N);
@@ -1912,7 +2011,7 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
         }
     }
     sc.triangles = T;
-    up(tri_mesh.data(), T * 4ull, sc.tri_mesh);
+    up(tri_mesh, T * 4ull, sc.tri_mesh);
     sc.light_count = (uint32_t)h.lights.size();
     sc.local_lights = h.local_lights;
     up(h.lights.data(), h.lights.size() * sizeof(DevLight), sc.lights);
@@ -2762,69 +2861,6 @@ dl_status run(dl_session &s, dl_progress *progress) {
         progress->stage = 4;
     }
     return DL_OK;
-}
-
-// Host buffers of freed results' words, handed to the next result. They are pinned (page-locked)
-// when the driver allows it, so that the download runs as a DMA copy at the link's rate instead
-// of through the driver's staging buffers, and a reused buffer needs no first-touch page faults
-// either. At most kCacheBytes are held.
-struct WordCache {
-    static constexpr size_t kCacheBytes = size_t(2) << 30;
-    struct Buffer {
-        size_t cap;  // words
-        uint32_t *p;
-        bool pinned;
-    };
-    std::mutex lock;
-    std::vector<Buffer> free;
-    size_t held = 0;
-    static void release(const Buffer &b) {
-        if (b.pinned) cudaFreeHost(b.p);  // fails harmlessly once the runtime has shut down at exit
-        else delete[] b.p;
-    }
-    Buffer take(size_t n) {
-        {
-            std::lock_guard<std::mutex> guard(lock);
-            size_t best = free.size();
-            for (size_t i = 0; i < free.size(); ++i)
-                if (free[i].cap >= n && (best == free.size() || free[i].cap < free[best].cap)) best = i;
-            if (best < free.size()) {
-                Buffer b = free[best];
-                free.erase(free.begin() + best);
-                held -= b.cap * 4;
-                return b;
-            }
-        }
-        size_t cap = n ? n : 1;
-        void *p = nullptr;
-        if (cudaHostAlloc(&p, cap * 4, cudaHostAllocPortable) == cudaSuccess) return Buffer{cap, (uint32_t *)p, true};
-        cudaGetLastError();  // no pinned memory to be had: a pageable buffer (a slower copy)
-        return Buffer{cap, new uint32_t[cap], false};
-    }
-    void clear() {
-        std::lock_guard<std::mutex> guard(lock);
-        for (const Buffer &b : free) release(b);
-        free.clear();
-        held = 0;
-    }
-    void give(const Buffer &b) {
-        std::lock_guard<std::mutex> guard(lock);
-        while (held + b.cap * 4 > kCacheBytes && !free.empty()) {  // drop the oldest
-            held -= free.front().cap * 4;
-            release(free.front());
-            free.erase(free.begin());
-        }
-        if (b.cap * 4 > kCacheBytes) {
-            release(b);
-            return;
-        }
-        free.push_back(b);
-        held += b.cap * 4;
-    }
-};
-WordCache &word_cache() {
-    static WordCache *c = new WordCache;  // never destroyed: results may be freed during exit
-    return *c;
 }
 
 // The result in one host allocation: the scene struct, its arrays, then the words.

@@ -83,3 +83,10 @@ def test_argument_errors_are_named_without_a_gpu():
     assert lib.dl_last_error() == b"the window does not lie inside the map"
     assert lib.dl_filter_bounce_window_noalloc(buf_a, buf_a, *args) == invalid_argument
     assert b"distinct" in lib.dl_last_error()
+    # the cache-bandwidth probe checks its level, size and passes before it touches a device
+    gbs = C.c_double(-1.0)
+    for level, size, passes in ((0, 1 << 26, 1), (3, 1 << 26, 1), (2, 1 << 10, 1), (2, 1 << 26, 0),
+                                (1, (1 << 32) + 16, 1)):
+        assert lib.dl_probe_read_bandwidth(0, level, C.c_uint64(size), passes, C.byref(gbs)) == invalid_argument
+        assert b"dl_probe_read_bandwidth" in lib.dl_last_error()
+    assert lib.dl_probe_read_bandwidth(0, 2, C.c_uint64(1 << 26), 1, null) == invalid_argument
