@@ -1044,6 +1044,7 @@ __global__ void k_pack_bounce(DevScene sc, uint32_t entries, const uint32_t *ent
     uint32_t t = pair_tri[p], s = pair_light[p];
     uint32_t m = sc.tri_mesh[t];
     const DevLight &l = sc.lights[s];
+    if (l.bounce_bits == 8) return;  // undithered: k_pack_bounce8
     size_t re = (size_t)m * sc.light_count + s;
     Rect w = bounce_window(region_rect + re * 4, sc.mesh_res[m]);
     uint32_t ww = w.max_x - w.min_x + 1;
@@ -1093,6 +1094,56 @@ __global__ void k_pack_bounce(DevScene sc, uint32_t entries, const uint32_t *ent
         }
     }
     if (colored ? acc_bits > 0 : (n % per) != 0) words[out++] = (uint32_t)acc;
+}
+
+// pack_bounce(_rgb) for 8-bit bounce (bounce_pack.rs:28-86), which has no dither (its amplitude
+// is 0, so no random draw is taken): every pixel quantizes on its own, so a warp packs one entry,
+// each lane four consecutive pixels — one word of four 8-bit pixels, or three words of four
+// 24-bit RGB pixels — in the padded crop grid's row-major order, as the sequential packer does.
+__global__ void k_pack_bounce8(DevScene sc, uint32_t entries, const uint32_t *entry_pair,
+                               const unsigned long long *entry_bdst, const uint32_t *pair_tri,
+                               const uint32_t *pair_light, const uint4 *tri_crop, const uint32_t *region_rect,
+                               const uint32_t *woff, const float4 *map, uint32_t *words) {
+    const uint32_t e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = lane_id();
+    if (e >= entries) return;  // uniform across the warp
+    const unsigned long long dst = entry_bdst[e];
+    if (dst == ~0ull) return;
+    const uint32_t p = entry_pair[e], t = pair_tri[p], s = pair_light[p], m = sc.tri_mesh[t];
+    const DevLight &l = sc.lights[s];
+    if (l.bounce_bits != 8) return;  // dithered: k_pack_bounce
+    const size_t re = (size_t)m * sc.light_count + s;
+    const Rect w = bounce_window(region_rect + re * 4, sc.mesh_res[m]);
+    const uint32_t ww = w.max_x - w.min_x + 1, base = woff[re];
+    const uint4 c = tri_crop[t];
+    const int gw = (int)(c.z - c.x + 5), gh = (int)(c.w - c.y + 5);
+    const uint64_t n = (uint64_t)gw * gh;
+    const bool colored = sc.colored_bounce != 0;
+    const uint64_t nwords = colored ? (n * 24 + 31) / 32 : (n + 3) / 4;
+    Pcg none{0, 0};  // never drawn from at 8 bits
+    for (uint64_t g = lane; g * 4 < n; g += 32) {
+        uint32_t px[4];
+        for (int k = 0; k < 4; ++k) {
+            const uint64_t i = g * 4 + k;
+            float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            const int gx = (int)(i % gw), gy = (int)(i / gw);
+            if (i < n && gx >= 2 && gy >= 2 && gx < gw - 2 && gy < gh - 2) {
+                const uint32_t x = c.x + gx - 2, y = c.y + gy - 2;
+                v = map[base + (size_t)(y - w.min_y) * ww + (x - w.min_x)];
+            }
+            px[k] = 0;
+            if (i < n) {
+                px[k] = quantize_bounce(v.x, 8, none);
+                if (colored) px[k] |= quantize_bounce(v.y, 8, none) << 8 | quantize_bounce(v.z, 8, none) << 16;
+            }
+        }
+        if (colored) {
+            const uint32_t out[3] = {px[0] | px[1] << 24, px[1] >> 8 | px[2] << 16, px[2] >> 16 | px[3] << 8};
+            for (int k = 0; k < 3; ++k)
+                if (g * 3 + k < nwords) words[dst + g * 3 + k] = out[k];
+        } else {
+            words[dst + g] = px[0] | px[1] << 8 | px[2] << 16 | px[3] << 24;
+        }
+    }
 }
 
 // ================================ optimize, seams, serialize ===========================
@@ -2812,7 +2863,10 @@ dl_status run(dl_session &s, dl_progress *progress) {
             k_pack_bounce<<<grid_for(kept), kBlock, 0, st>>>(sc, kept, entry_pair, entry_bdst, pair_tri, pair_light,
                                                              tri_crop, region_rect, woff, bmap, words);
             LAUNCHED("k_pack_bounce");
-            ++s.launches;
+            k_pack_bounce8<<<grid_for((size_t)kept * 32), kBlock, 0, st>>>(
+                sc, kept, entry_pair, entry_bdst, pair_tri, pair_light, tri_crop, region_rect, woff, bmap, words);
+            LAUNCHED("k_pack_bounce8");
+            s.launches += 2;
         }
     }
     CK(cudaEventRecord(s.marks[7], st));
