@@ -274,12 +274,20 @@ DL_HD void ff_sincos_poly(FF r, FF &s, FF &c) {
     s = ff_sin_poly(r, r2);
     c = ff_cos_poly(r2);
 }
-// Ziv's rounding test: true when every value within 2^-36 relative of h + l rounds to h.
+// Ziv's rounding test: true when every value within 2^-36 relative of h + l rounds to h. The
+// gaps to the neighbouring binary32 values come from h's exponent bits: 2^(e-23) away from zero,
+// and half that towards zero when h is a power of two (its binade's lower edge).
 DL_HD bool ff_rounds_to(FF v, float &out) {
     float a = fabsf(v.h);
     if (!(a >= 1.0e-30f && a < 1.0e30f)) return false;
-    float up = nextafterf(v.h, INFINITY) - v.h;
-    float down = v.h - nextafterf(v.h, -INFINITY);
+    uint32_t bits;
+    memcpy(&bits, &a, 4);
+    const uint32_t pow2 = bits & 0x7F800000u;
+    float ulp;
+    memcpy(&ulp, &pow2, 4);
+    ulp = ulp * 1.1920928955078125e-07f;  // 2^-23: exact, the result stays normal for a >= 1e-30
+    const float away = ulp, toward = (bits & 0x007FFFFFu) ? ulp : 0.5f * ulp;
+    const float up = v.h > 0.0f ? away : toward, down = v.h > 0.0f ? toward : away;
     float err = a * 1.4551915228366852e-11f;  // 2^-36, far above the path's 2^-40 error bound
     if (v.l + err < 0.5f * up && v.l - err > -0.5f * down) {
         out = v.h;
