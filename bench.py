@@ -308,6 +308,14 @@ def main():
     assert probe_lib.dl_probe_read_bandwidth(local, 1, L2_PROBE_BYTES, 400, C.byref(l1_gbs)) == 0, \
         probe_lib.dl_last_error()
 
+    traffic = g_traffic = None
+    traffic_path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(traffic_path):  # DRAM bytes per launch from an ncu capture (profiles/)
+        with open(traffic_path) as f:
+            captured = json.load(f)
+        entry, g_entry = captured.get(args.workload), captured.get(args.workload + ":k_gather")
+        traffic = entry["bytes_per_launch"] if entry else None
+        g_traffic = g_entry["bytes_per_launch"] if g_entry else None
     # the second hot kernel, the bounce gather: node visits x 64 B + triangle tests x 48 B of the
     # instrumented gather, plus per item the texel, face and value (52 B), over its event time
     gms = statistics.median(gather_ms)
@@ -321,7 +329,7 @@ def main():
             "peak_source": "the same L2 read bandwidth measurement",
             "limiter": "instruction issue (ncu on the quarter-size outdoor case: issue slots 71 % busy, "
                        "SIMT efficiency 40 %, L2 throughput 8.4 % of peak)",
-            "algorithmic_bytes_per_launch": int(g_bytes), "ms": gms,
+            "algorithmic_bytes_per_launch": int(g_bytes), "ms": gms, "traffic": g_traffic,
             "bytes_per_unit": "64 per node visit + 48 per triangle test + 52 per (bounce pair, texel) item",
             "node_visits": int(crep.gather_node_visits), "tri_tests": int(crep.gather_tri_tests),
             "items": int(rep.bounce_items)}
@@ -346,12 +354,6 @@ def main():
     hybrid_flips = compare.bit_flips(hybrid.result(), result)
     hybrid_masks_equal = all(v["flips"] == 0 for k, v in hybrid_flips.items() if k != "bounce")
     hybrid.close()
-    traffic = None
-    traffic_path = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(traffic_path):  # DRAM bytes per launch from an ncu capture (profiles/)
-        with open(traffic_path) as f:
-            entry = json.load(f).get(args.workload)
-        traffic = entry["bytes_per_launch"] if entry else None
 
     # end to end through the C ABI (dl_bake_ex) from host buffers: validation, BVH build,
     # uploads, the device pipeline and the download of every mesh's words, timed around the call
