@@ -2302,31 +2302,47 @@ GatherTune gather_tune(dl_session &s, BounceArgs ba, uint32_t bpairs, bool refin
     cudaEvent_t a, b;
     CK(cudaEventCreate(&a));
     CK(cudaEventCreate(&b));
-    float best_ms = INFINITY;
     auto t0 = std::chrono::steady_clock::now();
-    for (uint32_t minb : minbs) {
-        for (uint32_t w : lanes) {
-            uint32_t blocks = blocks_for(minb, w);
-            ba.lanes = w;
-            ba.buffered = gather_buffer(s.host, w);
-            ba.scratch = gather_scratch(s, blocks, w, ba.buffered);
-            CK(cudaMemsetAsync(ba.head, 0, sizeof(unsigned long long), st));
-            CK(cudaEventRecord(a, st));
-            gather_kernel(refine, minb)<<<blocks, kBlock, gather_smem(best.stack_depth, w, ba.buffered), st>>>(
-                s.sc, ba);
-            CK(cudaGetLastError());
-            CK(cudaEventRecord(b, st));
-            CK(cudaEventSynchronize(b));
-            float ms = 0.0f;
-            CK(cudaEventElapsedTime(&ms, a, b));
-            ++best.trials;
-            if (ms < best_ms) {
-                best_ms = ms;
-                best.lanes = w;
-                best.minb = minb;
-                best.blocks = blocks;
-                best.buffered = ba.buffered;
-            }
+    // One launch of a candidate shape over the sampled steps (every >= 2) or the whole queue.
+    auto trial = [&](uint32_t minb, uint32_t w, uint32_t sample) {
+        const uint32_t blocks = blocks_for(minb, w);
+        ba.lanes = w;
+        ba.buffered = gather_buffer(s.host, w);
+        ba.scratch = gather_scratch(s, blocks, w, ba.buffered);
+        ba.sample_every = sample;
+        CK(cudaMemsetAsync(ba.head, 0, sizeof(unsigned long long), st));
+        CK(cudaEventRecord(a, st));
+        gather_kernel(refine, minb)<<<blocks, kBlock, gather_smem(best.stack_depth, w, ba.buffered), st>>>(s.sc,
+                                                                                                            ba);
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(b, st));
+        CK(cudaEventSynchronize(b));
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, a, b));
+        ++best.trials;
+        return ms;
+    };
+    // The sampled trials shortlist two shapes; those two then run over the whole queue, and the
+    // faster wins. A sample has few steps per warp, so its load balance favours the finer
+    // shapes more than the whole pass does (sampled trials alone picked 8 lanes per texel on the
+    // outdoor gather, 3 % slower than the 4 lanes the whole pass prefers).
+    struct Candidate {
+        float ms;
+        uint32_t minb, w;
+    };
+    std::vector<Candidate> tried;
+    for (uint32_t minb : minbs)
+        for (uint32_t w : lanes) tried.push_back(Candidate{trial(minb, w, every), minb, w});
+    std::stable_sort(tried.begin(), tried.end(), [](const Candidate &x, const Candidate &y) { return x.ms < y.ms; });
+    float best_ms = INFINITY;
+    for (size_t k = 0; k < std::min<size_t>(2, tried.size()); ++k) {
+        const float ms = trial(tried[k].minb, tried[k].w, 1);
+        if (ms < best_ms) {
+            best_ms = ms;
+            best.lanes = tried[k].w;
+            best.minb = tried[k].minb;
+            best.blocks = blocks_for(tried[k].minb, tried[k].w);
+            best.buffered = gather_buffer(s.host, tried[k].w);
         }
     }
     cudaEventDestroy(a);
