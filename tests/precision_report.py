@@ -114,6 +114,7 @@ def main():
                    "generate_s": round(time.time() - t0, 2)}
     exact, exact_ms, exact_rep = timed(inp, opts, "batched", args.steps)
     refined, refined_ms, refined_rep = timed(inp, opts, "refined", args.steps)
+    hybrid, hybrid_ms, _ = timed(inp, opts, "bounce_refined", args.steps)
     rays = exact.stats["rays"] + exact.stats["bounce_rays"]
     flips = compare.bit_flips(refined, exact)
     out["full"].update({
@@ -121,7 +122,9 @@ def main():
         "batched_ms": exact_ms, "refined_ms": refined_ms,
         "batched_rays_per_s": rays / (exact_ms / 1e3), "refined_rays_per_s": rays / (refined_ms / 1e3),
         "refined_retests": int(refined_rep.retests),
-        "refined_vs_exact_flips": flips, "refined_vs_exact_flip_total": total(flips)})
+        "refined_vs_exact_flips": flips, "refined_vs_exact_flip_total": total(flips),
+        "bounce_refined_ms": hybrid_ms,
+        "bounce_refined_vs_exact_flips": compare.bit_flips(hybrid, exact)})
 
     # 2. the slice against both oracles
     inp, opts = scenes.precision_stress(**SLICE)
@@ -134,6 +137,10 @@ def main():
     sl["batched"] = {"flips_vs_reference": total(compare.bit_flips(scene, ref32["scene"])),
                      "flips_vs_fp64": compare.bit_flips(scene, ref64["scene"]),
                      "bounce_error_vs_fp64": compare.bounce_error(maps, ref64["maps"])}
+    scene, maps, _ = gpu_with_maps(inp, opts, "bounce_refined")
+    sl["bounce_refined"] = {"flips_vs_reference": compare.bit_flips(scene, ref32["scene"]),
+                            "flips_vs_fp64": compare.bit_flips(scene, ref64["scene"]),
+                            "bounce_error_vs_fp64": compare.bounce_error(maps, ref64["maps"])}
     sl["refined"] = {}
     for eps in EPSILONS:
         scene, maps, rep = gpu_with_maps(inp, opts, "refined", refine_epsilon=eps)
