@@ -602,19 +602,19 @@ struct BounceArgs {
 // (parallel rays towards the sun), marking blocked ones in a second mask; each open sample's
 // value then moves to its rank among the open samples (popcounts of the masks), and the group
 // loads those values W at a time while the leader adds them, in sample order, as the reference
-// does (sun_bounce.rs:70). Dynamic shared memory holds the traversal stacks, one float4
-// contribution slot per thread and the groups' masks. MINB is the launch bound's blocks per SM (the register budget: 6 leaves the compiler its 80 registers, 8 asks for 64).
+// does (sun_bounce.rs:70). Dynamic shared memory holds only the traversal stacks and the groups'
+// masks (the per-round contributions go to the leader by shuffles), so that the rest of each SM's
+// unified L1/shared memory stays L1 cache for the BVH. MINB is the launch bound's blocks per SM (the register budget: 6 leaves the compiler its 80 registers, 8 asks for 64).
 template <bool COUNT, bool REFINE, int MINB>
 __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs a) {
     extern __shared__ int smem[];
     int *my = smem + threadIdx.x;
-    float4 *part = reinterpret_cast<float4 *>(smem + (size_t)a.stack_depth * kBlock);
     const uint32_t lane = lane_id(), W = a.lanes, sub = lane % W, per_step = 32 / W;
     // this lane group's masks (shared memory: samples whose hit is lit, then those whose shadow
     // ray is blocked) and scratch (global memory) for aligned sun gathers
     const uint32_t group = (threadIdx.x >> 5) * per_step + lane / W, words = a.buffered / 32;
     const unsigned group_lanes = W == 32 ? 0xFFFFFFFFu : ((1u << W) - 1u) << (lane / W * W);
-    uint32_t *lit = reinterpret_cast<uint32_t *>(part + kBlock) + (size_t)group * 2 * words;
+    uint32_t *lit = reinterpret_cast<uint32_t *>(smem + (size_t)a.stack_depth * kBlock) + (size_t)group * 2 * words;
     uint32_t *blocked = lit + words;
     float4 *scratch = a.scratch + ((size_t)blockIdx.x * (kBlock / W) + group) * 2 * a.buffered;
     for (uint32_t w = sub; w < 2 * words; w += W) lit[w] = 0u;
@@ -701,15 +701,15 @@ __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs
                 }
                 rays += c.rays;
             }
-            part[threadIdx.x] = make_float4(c.value.x, c.value.y, c.value.z, c.add ? 1.0f : 0.0f);
-            __syncwarp(group_lanes);
-            if (sub == 0 && samples) {
-                for (uint32_t j = 0; j < W && r * W + j < samples; ++j) {
-                    float4 q = part[threadIdx.x + j];
-                    if (q.w != 0.0f) sum.add(f3{q.x, q.y, q.z});
-                }
+            // the leader adds the round's contributions in sample order, from the group's lanes
+            const uint32_t lane0 = lane - sub, n = samples > r * W ? min(W, samples - r * W) : 0u;
+            for (uint32_t j = 0; j < n; ++j) {
+                const float x = __shfl_sync(group_lanes, c.value.x, lane0 + j);
+                const float y = __shfl_sync(group_lanes, c.value.y, lane0 + j);
+                const float z = __shfl_sync(group_lanes, c.value.z, lane0 + j);
+                const int add = __shfl_sync(group_lanes, (int)c.add, lane0 + j);
+                if (sub == 0 && add) sum.add(f3{x, y, z});
             }
-            __syncwarp(group_lanes);
         }
         __syncwarp();
         if (aligned) {
@@ -2238,11 +2238,10 @@ GatherKernel gather_kernel(bool refine, uint32_t minb, bool count = false) {
     CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kGatherSmemMax));
     return k;
 }
-// Shared memory of a gather launch: stacks, the round slots and, for aligned sun gathers, two
-// masks of `buffered` bits per lane group.
+// Shared memory of a gather launch: stacks and, for aligned sun gathers, two masks of `buffered`
+// bits per lane group (kept small: what the block does not take stays L1 cache for the BVH).
 size_t gather_smem(uint32_t depth, uint32_t lanes, uint32_t buffered) {
-    return (size_t)depth * kBlock * sizeof(int) + kBlock * sizeof(float4) +
-           (size_t)(kBlock / lanes) * 2 * (buffered / 32) * sizeof(uint32_t);
+    return (size_t)depth * kBlock * sizeof(int) + (size_t)(kBlock / lanes) * 2 * (buffered / 32) * sizeof(uint32_t);
 }
 // The samples a lane group holds for aligned sun gathers: the largest power-of-two sun bounce
 // sample count from 32 to 256 (0 when there is none).
