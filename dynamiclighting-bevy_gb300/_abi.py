@@ -56,7 +56,8 @@ class DlBakeConfig(C.Structure):
                 ("chunk_texels", C.c_uint32), ("sample_lanes", C.c_uint32),
                 ("blocks_per_sm", C.c_uint32), ("count_visits", C.c_uint32),
                 ("refine_epsilon", C.c_float), ("no_autotune", C.c_uint32), ("host_bvh", C.c_uint32),
-                ("max_device_mib", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+                ("max_device_mib", C.c_uint32), ("min_blocks", C.c_uint32),
+                ("gather_min_blocks", C.c_uint32), ("reserved", C.c_uint32 * 1)]
 
 
 class DlBakeReport(C.Structure):
@@ -75,7 +76,8 @@ class DlBakeReport(C.Structure):
                 ("tune_trials", C.c_uint32), ("ms_tune", C.c_double),
                 ("tuned_gather_lanes", C.c_uint32), ("cancel_stops", C.c_uint32),
                 ("gather_node_visits", C.c_uint64), ("gather_tri_tests", C.c_uint64),
-                ("ms_gather", C.c_double), ("bounce_items", C.c_uint64)]
+                ("ms_gather", C.c_double), ("bounce_items", C.c_uint64),
+                ("tuned_gather_min_blocks", C.c_uint32), ("tuned_gather_blocks_per_sm", C.c_uint32)]
 
 
 class DlLightBvhNode(C.Structure):

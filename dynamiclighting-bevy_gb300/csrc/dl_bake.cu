@@ -1853,6 +1853,15 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
         g_error = "sample_lanes must be 0 or a power of two up to 32";
         return DL_INVALID_ARGUMENT;
     }
+    const uint32_t mb = s->config.min_blocks, gmb = s->config.gather_min_blocks;
+    if (!(mb == 0 || (mb >= 7 && mb <= 10) || mb == 12)) {
+        g_error = "min_blocks must be 0, 7, 8, 9, 10 or 12";
+        return DL_INVALID_ARGUMENT;
+    }
+    if (!(gmb == 0 || gmb == 6 || (gmb >= 8 && gmb <= 10))) {
+        g_error = "gather_min_blocks must be 0, 6, 8, 9 or 10";
+        return DL_INVALID_ARGUMENT;
+    }
     float eps = s->config.refine_epsilon;
     if (!(eps >= 0.0f && eps <= 0.01f)) {
         g_error = "refine_epsilon must lie in [0, 0.01]";
@@ -2108,11 +2117,15 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
 // else stays on the device until dl_session_result.
 // ---- launch-shape autotuner of the batched visibility kernel ---------------------------------
 // Knobs: chunk size (warp-steps per claimed chunk), sky sample lanes (lanes sharing one sky
-// texel), the launch bound's blocks per SM (register budget 72 or 64 per thread) and the stack
-// depth (the BVH's depth, rounded up; it sets the shared memory per block and so, with the
-// registers, the resident blocks). Each candidate runs on every k-th chunk of the real queue
-// (k = 8 from 4 M items, 4 from 1 M) with scratch counters; its results are the same levels the
-// real pass writes (OR and max), so the trials change no output. The fastest shape is cached per
+// texel), the launch bound's blocks per SM (the register budget: 7, 8, 9, 10 or 12 blocks of 128
+// threads give 72, 64, 56, 48 or 40 registers per thread) and the stack depth (the BVH's depth,
+// rounded up; it sets the shared memory per block and so, with the registers, the resident
+// blocks). Each candidate runs on every k-th chunk of the real queue (k = 8 from 4 M items, 4
+// from 1 M) with scratch counters; its results are the same levels the real pass writes (OR and
+// max), so the trials change no output. Chunk size and lanes are tried at 8 blocks per SM, then
+// the other register budgets with the winning pair (more warps hide more of the traversal's L1
+// and L2 latency, fewer registers spill more: on the outdoor scene 12 blocks ran the visibility
+// stage in 135.7 ms, 9 in 137.8, 10 in 139.4, 8 in 141.9). The fastest shape is cached per
 // process, keyed by the device and the queue's shape.
 struct TraceTune {
     uint32_t grab = 1, sky_lanes = 1, minb = 7, stack_depth = kStack, blocks = 1, trials = 0;
@@ -2123,16 +2136,23 @@ using TraceKernel = void (*)(DevScene, TraceArgs);
 TraceKernel trace_kernel(bool count, bool refine, uint32_t minb) {
     if (count) return refine ? k_trace_batched<true, true, 7> : k_trace_batched<true, false, 7>;
     if (refine) return k_trace_batched<false, true, 7>;
-    return minb == 8 ? k_trace_batched<false, false, 8> : k_trace_batched<false, false, 7>;
+    switch (minb) {
+        case 8: return k_trace_batched<false, false, 8>;
+        case 9: return k_trace_batched<false, false, 9>;
+        case 10: return k_trace_batched<false, false, 10>;
+        case 12: return k_trace_batched<false, false, 12>;
+        default: return k_trace_batched<false, false, 7>;
+    }
 }
 
 struct TuneKey {
     int device;
     uint64_t items, sky_items, pairs, occluders, nodes;
-    uint32_t depth, flags, fixed;
+    uint32_t depth, flags, fixed, fixed_minb;
     bool operator<(const TuneKey &o) const {
-        return std::tie(device, items, sky_items, pairs, occluders, nodes, depth, flags, fixed) <
-               std::tie(o.device, o.items, o.sky_items, o.pairs, o.occluders, o.nodes, o.depth, o.flags, o.fixed);
+        return std::tie(device, items, sky_items, pairs, occluders, nodes, depth, flags, fixed, fixed_minb) <
+               std::tie(o.device, o.items, o.sky_items, o.pairs, o.occluders, o.nodes, o.depth, o.flags, o.fixed,
+                        o.fixed_minb);
     }
 };
 std::mutex g_tune_lock;
@@ -2154,20 +2174,23 @@ TraceTune trace_tune(dl_session &s, TraceArgs ta, bool refine, bool count, dl_pr
     std::vector<uint32_t> lanes = c.sample_lanes ? std::vector<uint32_t>{c.sample_lanes}
                                   : ta.sky_items  ? std::vector<uint32_t>{1, 2, 4, 8, 16}
                                                   : std::vector<uint32_t>{1};
-    std::vector<uint32_t> minbs = (count || refine) ? std::vector<uint32_t>{7} : std::vector<uint32_t>{7, 8};
+    // the chunk and lane trials run at the first budget; untuned launches take 7 blocks per SM
+    std::vector<uint32_t> minbs = (count || refine) ? std::vector<uint32_t>{7}
+                                  : c.min_blocks    ? std::vector<uint32_t>{c.min_blocks}
+                                                    : std::vector<uint32_t>{8, 7, 9, 10, 12};
     const uint32_t every = ta.items >= (4u << 20) ? 8 : ta.items >= (1u << 20) ? 4 : 0;
     const bool tune = !c.no_autotune && every && grabs.size() * lanes.size() * minbs.size() > 1 &&
                       !(progress && progress->cancel);
     best.grab = grabs[0];
     best.sky_lanes = lanes[0];
-    best.minb = minbs[0];
+    best.minb = (count || refine || !c.min_blocks) ? 7u : c.min_blocks;
     if (!tune) {
         best.blocks = blocks_for(best.minb);
         return best;
     }
     TuneKey key{s.device, ta.items, ta.sky_items, ta.pairs, s.host.occ_mesh.size(), s.host.bvh_node_count,
                 best.stack_depth, (count ? 1u : 0u) | (refine ? 2u : 0u),
-                c.chunk_texels | (c.sample_lanes << 16) | (c.blocks_per_sm << 24)};
+                c.chunk_texels | (c.sample_lanes << 16) | (c.blocks_per_sm << 24), c.min_blocks};
     {
         std::lock_guard<std::mutex> guard(g_tune_lock);
         auto it = g_tune_cache.find(key);
@@ -2187,31 +2210,32 @@ TraceTune trace_tune(dl_session &s, TraceArgs ta, bool refine, bool count, dl_pr
     CK(cudaEventCreate(&b));
     float best_ms = INFINITY;
     auto t0 = std::chrono::steady_clock::now();
-    for (uint32_t minb : minbs) {
-        uint32_t blocks = blocks_for(minb);
-        for (uint32_t w : lanes)
-            for (uint32_t g : grabs) {
-                ta.grab = g;
-                ta.sky_lanes = w;
-                CK(cudaMemsetAsync(ta.head, 0, 2 * sizeof(unsigned long long), st));
-                CK(cudaEventRecord(a, st));
-                trace_kernel(count, refine, minb)<<<blocks, kBlock, (size_t)best.stack_depth * kBlock * sizeof(int),
-                                                     st>>>(s.sc, ta);
-                CK(cudaGetLastError());
-                CK(cudaEventRecord(b, st));
-                CK(cudaEventSynchronize(b));
-                float ms = 0.0f;
-                CK(cudaEventElapsedTime(&ms, a, b));
-                ++best.trials;
-                if (ms < best_ms) {
-                    best_ms = ms;
-                    best.grab = g;
-                    best.sky_lanes = w;
-                    best.minb = minb;
-                    best.blocks = blocks;
-                }
-            }
-    }
+    auto trial = [&](uint32_t minb, uint32_t w, uint32_t g) {
+        const uint32_t blocks = blocks_for(minb);
+        ta.grab = g;
+        ta.sky_lanes = w;
+        CK(cudaMemsetAsync(ta.head, 0, 2 * sizeof(unsigned long long), st));
+        CK(cudaEventRecord(a, st));
+        trace_kernel(count, refine, minb)<<<blocks, kBlock, (size_t)best.stack_depth * kBlock * sizeof(int), st>>>(
+            s.sc, ta);
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(b, st));
+        CK(cudaEventSynchronize(b));
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, a, b));
+        ++best.trials;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best.grab = g;
+            best.sky_lanes = w;
+            best.minb = minb;
+            best.blocks = blocks;
+        }
+    };
+    for (uint32_t w : lanes)
+        for (uint32_t g : grabs) trial(minbs[0], w, g);
+    const uint32_t w = best.sky_lanes, g = best.grab;
+    for (size_t k = 1; k < minbs.size(); ++k) trial(minbs[k], w, g);
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     best.ms = ms_since(t0);
@@ -2233,8 +2257,10 @@ constexpr int kGatherSmemMax = 80 * 1024;
 GatherKernel gather_kernel(bool refine, uint32_t minb, bool count = false) {
     GatherKernel k = count    ? k_gather<true, false, 6>
                      : refine ? k_gather<false, true, 6>
-                     : minb == 8 ? k_gather<false, false, 8>
-                                 : k_gather<false, false, 6>;
+                     : minb == 8  ? k_gather<false, false, 8>
+                     : minb == 9  ? k_gather<false, false, 9>
+                     : minb == 10 ? k_gather<false, false, 10>
+                                  : k_gather<false, false, 6>;
     CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kGatherSmemMax));
     return k;
 }
@@ -2274,16 +2300,20 @@ GatherTune gather_tune(dl_session &s, BounceArgs ba, uint32_t bpairs, bool refin
     };
     std::vector<uint32_t> lanes = c.sample_lanes ? std::vector<uint32_t>{c.sample_lanes}
                                                  : std::vector<uint32_t>{1, 4, 8, 16, 32};
-    std::vector<uint32_t> minbs = refine ? std::vector<uint32_t>{6} : std::vector<uint32_t>{6, 8};
+    // register budgets (blocks per SM: 6, 8, 9, 10 give 80, 64, 56, 48 registers per thread); the
+    // lane trials run at the first, the others with the two best lane counts
+    std::vector<uint32_t> minbs = refine                ? std::vector<uint32_t>{6}
+                                  : c.gather_min_blocks ? std::vector<uint32_t>{c.gather_min_blocks}
+                                                        : std::vector<uint32_t>{8, 6, 9, 10};
     const uint32_t every = ba.items >= (1u << 20) ? 8 : ba.items >= (1u << 18) ? 4 : 0;
     best.lanes = lanes[0];
-    best.minb = minbs[0];
+    best.minb = (refine || !c.gather_min_blocks) ? 6u : c.gather_min_blocks;  // untuned
     best.buffered = gather_buffer(s.host, best.lanes);
     best.blocks = blocks_for(best.minb, best.lanes);
     if (c.no_autotune || !every || lanes.size() * minbs.size() == 1 || (progress && progress->cancel))
         return best;
     TuneKey key{s.device, ba.items, bpairs, 0, s.host.occ_mesh.size(), s.host.bvh_node_count, best.stack_depth,
-                refine ? 2u : 0u, c.blocks_per_sm};
+                refine ? 2u : 0u, c.blocks_per_sm | (c.sample_lanes << 16), c.gather_min_blocks};
     {
         std::lock_guard<std::mutex> guard(g_tune_lock);
         auto it = g_gather_cache.find(key);
@@ -2324,15 +2354,22 @@ GatherTune gather_tune(dl_session &s, BounceArgs ba, uint32_t bpairs, bool refin
     // The sampled trials shortlist two shapes; those two then run over the whole queue, and the
     // faster wins. A sample has few steps per warp, so its load balance favours the finer
     // shapes more than the whole pass does (sampled trials alone picked 8 lanes per texel on the
-    // outdoor gather, 3 % slower than the 4 lanes the whole pass prefers).
+    // outdoor gather, 3 % slower than the 4 lanes the whole pass prefers). More resident warps
+    // hide more of the traversal's latency and fewer registers spill more: on the outdoor gather
+    // 10 blocks per SM ran in 93.4 ms, 9 in 94.3, 8 in 97.1, 12 (40 registers) in 102.3.
     struct Candidate {
         float ms;
         uint32_t minb, w;
     };
+    auto by_ms = [](const Candidate &x, const Candidate &y) { return x.ms < y.ms; };
     std::vector<Candidate> tried;
-    for (uint32_t minb : minbs)
-        for (uint32_t w : lanes) tried.push_back(Candidate{trial(minb, w, every), minb, w});
-    std::stable_sort(tried.begin(), tried.end(), [](const Candidate &x, const Candidate &y) { return x.ms < y.ms; });
+    for (uint32_t w : lanes) tried.push_back(Candidate{trial(minbs[0], w, every), minbs[0], w});
+    std::stable_sort(tried.begin(), tried.end(), by_ms);
+    const size_t lane_picks = std::min<size_t>(2, tried.size());
+    for (size_t m = 1; m < minbs.size(); ++m)
+        for (size_t k = 0; k < lane_picks; ++k)
+            tried.push_back(Candidate{trial(minbs[m], tried[k].w, every), minbs[m], tried[k].w});
+    std::stable_sort(tried.begin(), tried.end(), by_ms);
     float best_ms = INFINITY;
     for (size_t k = 0; k < std::min<size_t>(2, tried.size()); ++k) {
         const float ms = trial(tried[k].minb, tried[k].w, 1);
@@ -2468,7 +2505,7 @@ dl_status run(dl_session &s, dl_progress *progress) {
     s.report.tuned_chunk_texels = s.report.tuned_sample_lanes = s.report.tuned_blocks_per_sm = 0;
     s.report.tuned_stack_depth = s.report.tuned_min_blocks = s.report.tune_trials = 0;
     s.report.ms_tune = 0.0;
-    s.report.tuned_gather_lanes = 0;
+    s.report.tuned_gather_lanes = s.report.tuned_gather_min_blocks = s.report.tuned_gather_blocks_per_sm = 0;
     s.report.cancel_stops = 0;
     s.report.bounce_items = 0;
     if (T == 0) {
@@ -2770,6 +2807,8 @@ dl_status run(dl_session &s, dl_progress *progress) {
             ba.buffered = g.buffered;
             ba.scratch = gather_scratch(s, g.blocks, g.lanes, g.buffered);
             s.report.tuned_gather_lanes = g.lanes;
+            s.report.tuned_gather_min_blocks = g.minb;
+            s.report.tuned_gather_blocks_per_sm = g.blocks / (uint32_t)s.sms;
             s.report.tune_trials += g.trials;
             s.report.ms_tune += g.ms;
             CK(cudaMemsetAsync(ba.head, 0, sizeof(unsigned long long), st));

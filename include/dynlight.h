@@ -184,7 +184,13 @@ typedef struct dl_bake_config {
                                   scene, BVH and its build scratch, every stage's buffers. An
                                   allocation past it fails the call with DL_OUT_OF_MEMORY and
                                   frees what the bake held. 0: no cap */
-    uint32_t reserved[3];
+    uint32_t min_blocks;       /* register budget of the bit-exact visibility kernel, as the
+                                  blocks of 128 threads per SM it is compiled to fit: 7, 8, 9, 10
+                                  or 12 (72, 64, 56, 48 or 40 registers per thread), 0: tuned.
+                                  The refined and counting kernels have one budget (7) */
+    uint32_t gather_min_blocks; /* the same for the bit-exact bounce gather: 6, 8, 9 or 10 (80,
+                                  64, 56 or 48 registers), 0: tuned; the refined gather has one (6) */
+    uint32_t reserved[1];
 } dl_bake_config;
 
 /* Timings (device events, milliseconds) and counters of the last bake. */
@@ -227,6 +233,8 @@ typedef struct dl_bake_report {
     uint64_t gather_tri_tests;   /* triangle tests of the bounce gather (counting config only) */
     double ms_gather;            /* device time of the bounce gather kernel alone (0: no gather) */
     uint64_t bounce_items;       /* (bounce pair, texel) items of the gather queue */
+    uint32_t tuned_gather_min_blocks;   /* gather launch bound: blocks per SM its registers fit */
+    uint32_t tuned_gather_blocks_per_sm; /* gather blocks resident per SM in the launch */
 } dl_bake_report;
 
 /* LightBvhNode (src/bake/light_bvh.rs:16-22), 32 bytes. */

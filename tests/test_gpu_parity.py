@@ -226,6 +226,22 @@ def test_tuning_does_not_change_the_bytes():
         assert other.words_equal(base) and other.stats == base.stats, tuning
 
 
+def test_register_budgets_do_not_change_the_bytes():
+    # every register budget the tuners may pick (the same kernel compiled for 7 to 12 resident
+    # blocks per SM, spilling more at the smaller budgets) writes the default budget's bytes,
+    # sky, sun and both bounce kinds included
+    rooms = scenes.room_grid(rooms=1, lights=4, boxes_per_room=3, samples=24)
+    rooms[1].photon_cube_resolution = 48
+    outdoor = scenes.outdoor(grid=33, chunks=2, boxes=12, point_lights=2, sky_samples=32, bounce_samples=64)
+    for inp, opts in (rooms, outdoor):
+        base = dl.bake(inp, opts)
+        for m, gm in ((8, 8), (9, 9), (10, 10), (12, 6), (7, 10)):
+            report = dl._abi.DlBakeReport()
+            other = dl.bake(inp, opts, min_blocks=m, gather_min_blocks=gm, report=report)
+            assert_same(other, base)  # the words carry the packed bounce maps
+            assert report.tuned_min_blocks == m and report.tuned_gather_min_blocks == gm
+
+
 @pytest.mark.parametrize("lanes", [1, 2, 4, 8, 32])
 def test_sky_sample_lanes_do_not_change_the_bytes(lanes):
     # lanes sharing one sky texel's samples: an integer sum of open samples, so the same levels

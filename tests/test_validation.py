@@ -169,6 +169,10 @@ def test_invalid_tuning_is_an_argument_error():
     inp, opts = room()
     fails(inp, opts, "invalid argument", "sample_lanes", sample_lanes=3)
     fails(inp, opts, "invalid argument", "refine_epsilon", refine_epsilon=0.5)
+    for m in (1, 6, 11, 13):
+        fails(inp, opts, "invalid argument", "min_blocks", min_blocks=m)
+    for m in (1, 7, 11, 12):
+        fails(inp, opts, "invalid argument", "gather_min_blocks", gather_min_blocks=m)
 
 
 @pytest.mark.parametrize("mesh_id", [0, 1, 0xFFFFFFFFFFFFFFFF])
