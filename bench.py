@@ -401,6 +401,9 @@ def main():
                    "launch_shape": {"chunk_texels": rep.tuned_chunk_texels, "sample_lanes": rep.tuned_sample_lanes,
                                     "blocks_per_sm": rep.tuned_blocks_per_sm,
                                     "stack_depth": rep.tuned_stack_depth, "launch_bound_blocks": rep.tuned_min_blocks,
+                                    "gather_lanes": rep.tuned_gather_lanes,
+                                    "gather_blocks_per_sm": rep.tuned_gather_blocks_per_sm,
+                                    "gather_launch_bound_blocks": rep.tuned_gather_min_blocks,
                                     "autotune_trials": tune.tune_trials if tune else 0,
                                     "autotune_ms": tune.ms_tune if tune else 0.0},
                    "parallelism": f"replicas x{world}"},

@@ -2029,13 +2029,11 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
         std::vector<uint32_t> occ_leaf(N);
         for (uint32_t k = 0; k < N; ++k) {
             uint32_t occ;
-            std::memcpy(&occ, &h.tri_v0[k * 4 + 3], 4);
+            std::memcpy(&occ, &h.tris[k * 12 + 3], 4);
             occ_leaf[occ] = k;
         }
         up(h.nodes.data(), h.nodes.size() * sizeof(BvhNode), sc.nodes);
-        up(h.tri_v0.data(), h.tri_v0.size() * 4, sc.tri_v0);
-        up(h.tri_e1.data(), h.tri_e1.size() * 4, sc.tri_e1);
-        up(h.tri_e2.data(), h.tri_e2.size() * 4, sc.tri_e2);
+        up(h.tris.data(), h.tris.size() * 4, sc.tris);
         up(occ_leaf.data(), N * 4ull, sc.occ_leaf);
     } else {
         auto t_bvh = std::chrono::steady_clock::now();
@@ -2058,15 +2056,11 @@ dl_status create(const dl_bake_input *in, const dl_bake_options *o, const dl_bak
         h.bvh_depth = db.depth;
         h.bvh_node_count = db.node_count;
         sc.nodes = reinterpret_cast<const float4 *>(db.nodes);
-        sc.tri_v0 = db.tri_v0;
-        sc.tri_e1 = db.tri_e1;
-        sc.tri_e2 = db.tri_e2;
+        sc.tris = db.tris;
         sc.occ_leaf = db.occ_leaf;
         if (N == 0) {  // no occluders: small placeholders, which traversal never reads
             sc.nodes = dev_alloc<float4>(s->owned, s->stream, 4, bytes, &s->budget);
-            sc.tri_v0 = dev_alloc<float4>(s->owned, s->stream, 1, bytes, &s->budget);
-            sc.tri_e1 = dev_alloc<float4>(s->owned, s->stream, 1, bytes, &s->budget);
-            sc.tri_e2 = dev_alloc<float4>(s->owned, s->stream, 1, bytes, &s->budget);
+            sc.tris = dev_alloc<float4>(s->owned, s->stream, 3, bytes, &s->budget);
             sc.occ_leaf = dev_alloc<uint32_t>(s->owned, s->stream, 1, bytes, &s->budget);
         }
     }
@@ -3429,12 +3423,7 @@ dl_status dl_session_occluder_bvh(dl_session *s, void *nodes, uint64_t node_cap,
         uint64_t n = std::min<uint64_t>(node_cap, h.bvh_node_count);
         if (n) CK(cudaMemcpy(nodes, s->sc.nodes, n * sizeof(BvhNode), cudaMemcpyDeviceToHost));
         uint64_t t = std::min<uint64_t>(tri_cap, s->sc.occluders);
-        std::vector<float4> part(t);
-        for (int j = 0; j < 3 && t; ++j) {
-            const float4 *src = j == 0 ? s->sc.tri_v0 : j == 1 ? s->sc.tri_e1 : s->sc.tri_e2;
-            CK(cudaMemcpy(part.data(), src, t * sizeof(float4), cudaMemcpyDeviceToHost));
-            for (uint64_t k = 0; k < t; ++k) std::memcpy(triangles + k * 12 + j * 4, &part[k], sizeof(float4));
-        }
+        if (t) CK(cudaMemcpy(triangles, s->sc.tris, t * 3 * sizeof(float4), cudaMemcpyDeviceToHost));
         return DL_OK;
     })
 }

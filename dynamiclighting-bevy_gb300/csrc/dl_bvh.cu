@@ -679,9 +679,10 @@ __global__ void k_leaf_triangles(DeviceBvhInput in, const uint32_t *idx, DeviceB
         v[j] = f3{q[0], q[1], q[2]};
     }
     f3 e1 = sub(v[1], v[0]), e2 = sub(v[2], v[0]);
-    out.tri_v0[k] = make_float4(v[0].x, v[0].y, v[0].z, __uint_as_float(i));
-    out.tri_e1[k] = make_float4(e1.x, e1.y, e1.z, 0.0f);
-    out.tri_e2[k] = make_float4(e2.x, e2.y, e2.z, 0.0f);
+    float4 *t = out.tris + (size_t)k * 3;
+    t[0] = make_float4(v[0].x, v[0].y, v[0].z, __uint_as_float(i));
+    t[1] = make_float4(e1.x, e1.y, e1.z, 0.0f);
+    t[2] = make_float4(e2.x, e2.y, e2.z, 0.0f);
     out.occ_leaf[i] = k;
 }
 
@@ -843,9 +844,7 @@ void build_bvh_device(const DeviceBvhInput &in, const std::function<void *(size_
     }
     out.node_count = inner;
     out.nodes = static_cast<BvhNode *>(alloc((size_t)inner * sizeof(BvhNode)));
-    out.tri_v0 = static_cast<float4 *>(alloc((size_t)n * sizeof(float4)));
-    out.tri_e1 = static_cast<float4 *>(alloc((size_t)n * sizeof(float4)));
-    out.tri_e2 = static_cast<float4 *>(alloc((size_t)n * sizeof(float4)));
+    out.tris = static_cast<float4 *>(alloc((size_t)n * 3 * sizeof(float4)));
     out.occ_leaf = static_cast<uint32_t *>(alloc((size_t)n * 4));
     k_emit<<<g, kThreads, 0, stream>>>(L, out.nodes);
     k_leaf_triangles<<<blocks_for(n, kThreads), kThreads, 0, stream>>>(in, st.idx, out);

@@ -25,7 +25,7 @@ struct DeviceBvhInput {
 
 struct DeviceBvh {
     BvhNode *nodes = nullptr;  // depth-first, the root first, each left subtree before its right one
-    float4 *tri_v0 = nullptr, *tri_e1 = nullptr, *tri_e2 = nullptr;  // leaf order; v0.w: occluder bits
+    float4 *tris = nullptr;    // leaf order, 3 per triangle: v0 (w: occluder bits), e1, e2
     uint32_t *occ_leaf = nullptr;  // occluder -> its slot in leaf order
     uint32_t node_count = 0;
     uint32_t depth = 0;        // the deepest node's level, the root being 1

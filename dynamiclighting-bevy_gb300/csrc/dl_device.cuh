@@ -18,7 +18,9 @@ namespace dl {
 struct DevScene {
     // BVH and triangles in leaf order
     const float4 *nodes;  // 4 float4 per node
-    const float4 *tri_v0, *tri_e1, *tri_e2;
+    // triangles as 3 float4 each, one 48-byte record per triangle (a leaf's triangles are
+    // contiguous): v0 (w: occluder index bits), e1 = v1 - v0, e2 = v2 - v0
+    const float4 *tris;
     uint32_t occluders;
     // occluder index -> mesh, triangle in mesh, position in leaf order
     const uint32_t *occ_mesh, *occ_tri, *occ_leaf;
@@ -274,12 +276,12 @@ __device__ bool traverse(const DevScene &sc, f3 o, f3 dir, float max, bool alpha
             uint32_t first = packed >> 3, count = packed & 7u;
             for (uint32_t k = 0; k < count; ++k) {
                 uint32_t i = first + k;
-                float4 v0 = ldg4(sc.tri_v0 + i);
+                const float4 *tp = sc.tris + (size_t)i * 3;
+                float4 v0 = ldg4(tp);
                 if (COUNT) ++vis->tris;
                 float t, u, v;
-                bool ok = REFINE ? tri_test_refined(sc, v0, ldg4(sc.tri_e1 + i), ldg4(sc.tri_e2 + i), o, d, max, t, u,
-                                                    v, vis)
-                                 : tri_test(v0, ldg4(sc.tri_e1 + i), ldg4(sc.tri_e2 + i), o, d, max, t, u, v);
+                bool ok = REFINE ? tri_test_refined(sc, v0, ldg4(tp + 1), ldg4(tp + 2), o, d, max, t, u, v, vis)
+                                 : tri_test(v0, ldg4(tp + 1), ldg4(tp + 2), o, d, max, t, u, v);
                 if (!ok) continue;
                 uint32_t occ = __float_as_uint(v0.w);
                 // the refined form orders closest-hit candidates by their binary64 distance (and

@@ -605,9 +605,7 @@ struct Builder {
 void build_bvh(HostScene &s) {
     size_t n = s.occ_mesh.size();
     s.nodes.clear();
-    s.tri_v0.assign(n * 4, 0.0f);
-    s.tri_e1.assign(n * 4, 0.0f);
-    s.tri_e2.assign(n * 4, 0.0f);
+    s.tris.assign(n * 12, 0.0f);
     if (n == 0) return;
     Builder b;
     b.prims.resize(n);
@@ -669,7 +667,7 @@ void build_bvh(HostScene &s) {
             uint32_t bits = i;
             float w;
             std::memcpy(&w, &bits, 4);
-            float *p0 = &s.tri_v0[k * 4], *p1 = &s.tri_e1[k * 4], *p2 = &s.tri_e2[k * 4];
+            float *p0 = &s.tris[k * 12], *p1 = p0 + 4, *p2 = p0 + 8;
             p0[0] = a.x; p0[1] = a.y; p0[2] = a.z; p0[3] = w;
             p1[0] = e1.x; p1[1] = e1.y; p1[2] = e1.z; p1[3] = 0.0f;
             p2[0] = e2.x; p2[1] = e2.y; p2[2] = e2.z; p2[3] = 0.0f;

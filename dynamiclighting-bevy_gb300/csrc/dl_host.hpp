@@ -71,7 +71,7 @@ struct HostScene {
     std::vector<uint32_t> occ_mesh, occ_tri;
     // BVH over the occluders, triangles in leaf order
     std::vector<BvhNode> nodes;
-    std::vector<float> tri_v0, tri_e1, tri_e2;  // 4 floats each (w of v0: occluder index bits)
+    std::vector<float> tris;  // 12 floats per triangle: v0 (w: occluder index bits), e1, e2
     uint32_t bvh_depth = 0;
     uint32_t bvh_node_count = 0;  // inner nodes, from either builder (the device one fills no vectors)
 };

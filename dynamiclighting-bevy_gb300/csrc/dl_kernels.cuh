@@ -360,7 +360,8 @@ __device__ __forceinline__ bool is_buried(const DevScene &sc, f3 normal, f3 orig
         bool backface = false;
         if (traverse<false, false, REFINE>(sc, origin, dir, INFINITY, false, stack, stride, h, vis)) {
             // face normal of the hit occluder: cross(b - a, c - a), normalized
-            float4 e1 = ldg4(sc.tri_e1 + sc.occ_leaf[h.occluder]), e2 = ldg4(sc.tri_e2 + sc.occ_leaf[h.occluder]);
+            const float4 *tp = sc.tris + (size_t)sc.occ_leaf[h.occluder] * 3;
+            float4 e1 = ldg4(tp + 1), e2 = ldg4(tp + 2);
             f3 fn = normalize_or_zero(cross(f3{e1.x, e1.y, e1.z}, f3{e2.x, e2.y, e2.z}));
             backface = dot(fn, dir) > 0.0f;
         }
@@ -434,7 +435,7 @@ __device__ __forceinline__ uint32_t cube_texel_index(f3 d, uint32_t res) {
 // Occluder::face_normal / surface_normal / albedo (occluder.rs:117-144) at a closest hit.
 __device__ __forceinline__ f3 hit_face_normal(const DevScene &sc, const Hit &h) {
     uint32_t leaf = sc.occ_leaf[h.occluder];
-    float4 e1 = ldg4(sc.tri_e1 + leaf), e2 = ldg4(sc.tri_e2 + leaf);
+    float4 e1 = ldg4(sc.tris + (size_t)leaf * 3 + 1), e2 = ldg4(sc.tris + (size_t)leaf * 3 + 2);
     return normalize_or_zero(cross(f3{e1.x, e1.y, e1.z}, f3{e2.x, e2.y, e2.z}));
 }
 __device__ __forceinline__ f3 hit_surface_normal(const DevScene &sc, const Hit &h, f3 face) {

@@ -33,7 +33,7 @@ static uint32_t walk(const HostScene &s, int32_t ref, const Box &box, std::vecto
         CHECK(count >= 1 && first + count <= seen.size(), "bad leaf %u %u\n", first, count);
         for (uint32_t k = first; k < first + count && k < seen.size(); ++k) {
             ++seen[k];
-            const float *v0 = &s.tri_v0[k * 4], *e1 = &s.tri_e1[k * 4], *e2 = &s.tri_e2[k * 4];
+            const float *v0 = &s.tris[k * 12], *e1 = v0 + 4, *e2 = v0 + 8;
             float p[3][3];
             for (int a = 0; a < 3; ++a) {
                 p[0][a] = v0[a];
@@ -110,7 +110,7 @@ int main(int argc, char **argv) {
     std::vector<int> occ(n, 0);
     for (size_t k = 0; k < n; ++k) {
         uint32_t o;
-        std::memcpy(&o, &s.tri_v0[k * 4 + 3], 4);
+        std::memcpy(&o, &s.tris[k * 12 + 3], 4);
         CHECK(o < n, "bad occluder index\n");
         if (o < n) ++occ[o];
     }
