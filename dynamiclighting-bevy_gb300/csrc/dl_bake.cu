@@ -604,7 +604,8 @@ struct BounceArgs {
 // loads those values W at a time while the leader adds them, in sample order, as the reference
 // does (sun_bounce.rs:70). Dynamic shared memory holds only the traversal stacks and the groups'
 // masks (the per-round contributions go to the leader by shuffles), so that the rest of each SM's
-// unified L1/shared memory stays L1 cache for the BVH. MINB is the launch bound's blocks per SM (the register budget: 6 leaves the compiler its 80 registers, 8 asks for 64).
+// unified L1/shared memory stays L1 cache for the BVH. MINB is the launch bound's blocks per SM
+// (the register budget: 6, 8, 9 and 10 give 80, 64, 56 and 48 registers a thread).
 template <bool COUNT, bool REFINE, int MINB>
 __global__ void __launch_bounds__(kBlock, MINB) k_gather(DevScene sc, BounceArgs a) {
     extern __shared__ int smem[];
@@ -2250,7 +2251,7 @@ using GatherKernel = void (*)(DevScene, BounceArgs);
 constexpr int kGatherSmemMax = 80 * 1024;
 GatherKernel gather_kernel(bool refine, uint32_t minb, bool count = false) {
     GatherKernel k = count    ? k_gather<true, false, 6>
-                     : refine ? k_gather<false, true, 6>
+                     : refine ? k_gather<false, true, 8>
                      : minb == 8  ? k_gather<false, false, 8>
                      : minb == 9  ? k_gather<false, false, 9>
                      : minb == 10 ? k_gather<false, false, 10>
@@ -2296,12 +2297,14 @@ GatherTune gather_tune(dl_session &s, BounceArgs ba, uint32_t bpairs, bool refin
                                                  : std::vector<uint32_t>{1, 4, 8, 16, 32};
     // register budgets (blocks per SM: 6, 8, 9, 10 give 80, 64, 56, 48 registers per thread); the
     // lane trials run at the first, the others with the two best lane counts
-    std::vector<uint32_t> minbs = refine                ? std::vector<uint32_t>{6}
+    std::vector<uint32_t> minbs = refine                ? std::vector<uint32_t>{8}
                                   : c.gather_min_blocks ? std::vector<uint32_t>{c.gather_min_blocks}
                                                         : std::vector<uint32_t>{8, 6, 9, 10};
     const uint32_t every = ba.items >= (1u << 20) ? 8 : ba.items >= (1u << 18) ? 4 : 0;
     best.lanes = lanes[0];
-    best.minb = (refine || !c.gather_min_blocks) ? 6u : c.gather_min_blocks;  // untuned
+    // untuned: 6 blocks per SM; the refined gather always takes 8 (64 registers: 173 ms on the
+    // outdoor scene against 178 ms at 80 registers and 173 ms at 48, its binary64 re-tests spill)
+    best.minb = refine ? 8u : c.gather_min_blocks ? c.gather_min_blocks : 6u;
     best.buffered = gather_buffer(s.host, best.lanes);
     best.blocks = blocks_for(best.minb, best.lanes);
     if (c.no_autotune || !every || lanes.size() * minbs.size() == 1 || (progress && progress->cancel))

@@ -189,7 +189,7 @@ typedef struct dl_bake_config {
                                   or 12 (72, 64, 56, 48 or 40 registers per thread), 0: tuned.
                                   The refined and counting kernels have one budget (7) */
     uint32_t gather_min_blocks; /* the same for the bit-exact bounce gather: 6, 8, 9 or 10 (80,
-                                  64, 56 or 48 registers), 0: tuned; the refined gather has one (6) */
+                                  64, 56 or 48 registers), 0: tuned; the refined gather has one (8) */
     uint32_t reserved[1];
 } dl_bake_config;
 
